@@ -1,0 +1,224 @@
+"""Generate the golden fixtures in this directory from the REFERENCE itself.
+
+Run (needs the reference source tree; it is imported, never copied):
+
+    HOME=$PWD/_work/home python tests/golden/make_golden.py /path/to/reference
+
+The script imports ``tupan.lib.extensions`` from the reference, which builds
+the reference's own C kernels through its cffi backend
+(``tupan/lib/cffi_backend.py:31-87``), and calls every extension through the
+reference's public ``calc`` API (``tupan/lib/extensions.py:94-97``) on seeded
+inputs.  Inputs and outputs are stored in ``golden_<case>.npz``; the sha256 of
+every reference source file used is stored with them.
+
+Cases follow the reference's own test (``tupan/tests/test_extensions.py``):
+uniform masses and x10 positions/velocities with eps2=0 at N=256, j-prefix
+and swapped i/j roles, eta=1/64, PN order 7 with c=128, dt=1/64; plus a
+softened Plummer sphere and a set of close two-body systems that drive the
+Sakura/Kepler solver through its Kepler branch, its period reduction, the
+hyperbolic start and the softened energy check.
+"""
+
+import glob
+import hashlib
+import os
+import sys
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+
+ATTRS = ("mass", "rx", "ry", "rz", "eps2", "vx", "vy", "vz",
+         "ax", "ay", "az", "jx", "jy", "jz")
+SHORT = {"mass": "m", "eps2": "e2"}
+
+
+class Bodies(object):
+    """Duck-typed particle set: the attributes the extensions read, plus
+    ``register_auxiliary_attribute`` (tupan/particles/allparticles.py:64)."""
+
+    def __init__(self, arrays, dtype):
+        self.n = len(arrays["m"])
+        self._dtype = dtype
+        for a in ATTRS:
+            setattr(self, a, np.ascontiguousarray(arrays[SHORT.get(a, a)],
+                                                  dtype=dtype).copy())
+
+    def register_auxiliary_attribute(self, name, kind):
+        setattr(self, name, np.zeros(self.n, dtype=self._dtype))
+
+
+def uniform(n, rng):
+    """tupan/tests/test_extensions.py:28-36 with a seeded generator."""
+    d = {"m": rng.random(n), "e2": np.zeros(n)}
+    d["rx"], d["ry"], d["rz"] = rng.random((n, 3)).T * 10
+    d["vx"], d["vy"], d["vz"] = rng.random((n, 3)).T * 10
+    for k in ("ax", "ay", "az", "jx", "jy", "jz"):
+        d[k] = rng.standard_normal(n)
+    return d
+
+
+def plummer(n, eps, rng):
+    """Small Plummer sphere (analytic potential, N-body units, G=M=1) with
+    per-particle eps2 = eps^2/2 as tupan/ics/plummer.py:62-63 stores it."""
+    m = np.full(n, 1.0 / n)
+    x = rng.random(n) * 0.999
+    r = 1.0 / np.sqrt(x ** (-2.0 / 3.0) - 1.0)
+    ct = rng.uniform(-1, 1, n)
+    ph = rng.uniform(0, 2 * np.pi, n)
+    st = np.sqrt(1 - ct ** 2)
+    pos = np.stack([r * st * np.cos(ph), r * st * np.sin(ph), r * ct])
+    q = np.empty(n)
+    k = 0
+    while k < n:
+        a, b = rng.random(2)
+        if b < a:
+            q[k] = b
+            k += 1
+    v = np.sqrt(-2 * q * (-1.0 / np.sqrt(1 + r * r)))
+    ct = rng.uniform(-1, 1, n)
+    ph = rng.uniform(0, 2 * np.pi, n)
+    st = np.sqrt(1 - ct ** 2)
+    vel = np.stack([v * st * np.cos(ph), v * st * np.sin(ph), v * ct])
+    s = 3 * np.pi / 16
+    pos *= s
+    vel /= np.sqrt(s)
+    d = {"m": m, "e2": np.full(n, eps * eps / 2)}
+    d["rx"], d["ry"], d["rz"] = pos
+    d["vx"], d["vy"], d["vz"] = vel
+    for c in ("ax", "ay", "az", "jx", "jy", "jz"):
+        d[c] = rng.standard_normal(n)
+    return d
+
+
+def close_pairs(rng, n_pairs):
+    """Interleaved two-body systems: bound, near-parabolic and hyperbolic
+    pairs at small separation (Kepler branch of twobody_solver,
+    sakura_kernel_common.h:111-122), widely separated from one another."""
+    d = {k: [] for k in ("m", "e2", "rx", "ry", "rz", "vx", "vy", "vz")}
+    for p in range(n_pairs):
+        m1, m2 = rng.uniform(0.1, 1.0, 2) * 1e-2
+        sep = rng.uniform(1e-3, 5e-2)
+        mu = m1 + m2
+        vc = np.sqrt(mu / sep)
+        kind = p % 4
+        fac = [0.3, 0.9, 1.4142, 2.5][kind] * rng.uniform(0.8, 1.2)
+        u = rng.standard_normal(3)
+        u /= np.linalg.norm(u)
+        w = rng.standard_normal(3)
+        w -= w.dot(u) * u
+        w /= np.linalg.norm(w)
+        rel_r = sep * u
+        rel_v = fac * vc * (w * 0.9 + u * 0.1 * rng.standard_normal())
+        centre = rng.uniform(-50, 50, 3)
+        for (mm, sgn, mo) in ((m1, 1, m2), (m2, -1, m1)):
+            d["m"].append(mm)
+            d["e2"].append(0.0 if p % 3 else 1e-8)
+            pos = centre + sgn * rel_r * mo / mu
+            vel = sgn * rel_v * mo / mu
+            d["rx"].append(pos[0]); d["ry"].append(pos[1]); d["rz"].append(pos[2])
+            d["vx"].append(vel[0]); d["vy"].append(vel[1]); d["vz"].append(vel[2])
+    out = {k: np.array(v) for k, v in d.items()}
+    n = len(out["m"])
+    for c in ("ax", "ay", "az", "jx", "jy", "jz"):
+        out[c] = rng.standard_normal(n)
+    return out
+
+
+def subset(d, sl):
+    return {k: v[sl] for k, v in d.items()}
+
+
+def main(refroot):
+    sys.path.insert(0, refroot)
+    from tupan.lib import extensions as ext
+
+    src = sorted(glob.glob(os.path.join(refroot, "tupan/lib/src/*")))
+    digests = {os.path.relpath(p, refroot):
+               hashlib.sha256(open(p, "rb").read()).hexdigest() for p in src}
+    for f in ("tupan/lib/extensions.py", "tupan/lib/cffi_backend.py"):
+        digests[f] = hashlib.sha256(
+            open(os.path.join(refroot, f), "rb").read()).hexdigest()
+
+    ext.clight.pn_order = 7
+    ext.clight.clight = 128
+
+    kernels = [
+        ("phi_kernel", ext.Phi, ()),
+        ("acc_kernel", ext.Acc, ()),
+        ("acc_jerk_kernel", ext.AccJerk, ()),
+        ("snap_crackle_kernel", ext.SnapCrackle, ()),
+        ("tstep_kernel", ext.Tstep, (1.0 / 64,)),
+        ("pnacc_kernel", ext.PNAcc, ()),
+        ("nreg_Xkernel", ext.NREG_X, (1.0 / 64,)),
+        ("nreg_Vkernel", ext.NREG_V, (1.0 / 64,)),
+        ("sakura_kernel", ext.Sakura, (1.0 / 64, 0)),
+        ("sakura_kernel", ext.Sakura, (1.0 / 64, -1)),
+        ("sakura_kernel", ext.Sakura, (1.0 / 64, 1)),
+        ("sakura_kernel", ext.Sakura, (1.0 / 64, -2)),
+        ("sakura_kernel", ext.Sakura, (1.0 / 64, 2)),
+    ]
+
+    rng = np.random.default_rng(20240611)
+    sets = {
+        "uniform256": uniform(256, rng),
+        "plummer96": plummer(96, 1e-2, rng),
+        "pairs": close_pairs(rng, 48),
+    }
+    roles = {
+        "uniform256": [("all", "all"), ("all", "j37"), ("i37", "all"),
+                       ("i1", "all")],
+        "plummer96": [("all", "all"), ("i5", "all")],
+        "pairs": [("all", "all")],
+    }
+    cut = {"all": slice(None), "j37": slice(0, 37), "i37": slice(0, 37),
+           "i5": slice(0, 5), "i1": slice(0, 1)}
+
+    for prec in ("float64", "float32"):
+        dtype = np.float64 if prec == "float64" else np.float32
+        for sname, data in sets.items():
+            store = {"__prec__": np.array(prec)}
+            for k, v in data.items():
+                store["in/" + k] = np.asarray(v, dtype=dtype)
+            for (ir, jr) in roles[sname]:
+                for (kname, cls, args) in kernels:
+                    # Fresh particle sets per call: extensions write their
+                    # results into i-attributes (e.g. Acc into ax/ay/az) that
+                    # later kernels read as inputs.
+                    I = Bodies(subset(data, cut[ir]), dtype)
+                    J = Bodies(subset(data, cut[jr]), dtype)
+                    kern = cls("C", prec)
+                    res = kern.calc(I, J, *args)
+                    tag = "%s|%s|%s|%s" % (kname, ir, jr,
+                                           ",".join(repr(a) for a in args))
+                    for idx, r in enumerate(res):
+                        store["out/%s/%d" % (tag, idx)] = np.array(r, copy=True)
+            if sname == "pairs":
+                # Kepler extension: each pair on its own, in place
+                # (tupan/lib/extensions.py:618-651).
+                # Softened pairs only at the short step: with a long step the
+                # reference's energy-check subdivision never terminates on
+                # them (universal_kepler_solver.h:580-606 has no bound).
+                n = len(data["m"]) // 2
+                soft = np.asarray(data["e2"])[0::2] > 0
+                for dt in (1.0 / 64, 1.0, 37.5):
+                    pairs = [p for p in range(n) if dt < 0.1 or not soft[p]]
+                    store["kepler_pairs/%r" % dt] = np.array(pairs)
+                    res = np.empty((len(pairs), 12), dtype=dtype)
+                    for row, p in enumerate(pairs):
+                        P = Bodies(subset(data, slice(2 * p, 2 * p + 2)),
+                                   dtype)
+                        kern = ext.Kepler("C", prec)
+                        kern.calc(P, P, dt)
+                        res[row] = np.concatenate(
+                            [P.rx, P.ry, P.rz, P.vx, P.vy, P.vz])
+                    store["kepler/%r" % dt] = res
+            store["__sources__"] = np.array(
+                "\n".join("%s %s" % (v, k) for k, v in sorted(digests.items())))
+            fn = os.path.join(HERE, "golden_%s_%s.npz" % (sname, prec))
+            np.savez_compressed(fn, **store)
+            print("wrote", fn, os.path.getsize(fn))
+
+
+if __name__ == "__main__":
+    main(sys.argv[1] if len(sys.argv) > 1 else "/root/reference")
