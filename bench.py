@@ -1,0 +1,387 @@
+"""Benchmark: Acc + AccJerk force sweeps at N = 262144 in SPLIT mode.
+
+One step = one Acc sweep and one AccJerk sweep of all N i-particles against
+all N j-particles of a seeded Plummer sphere (equal masses, eps = 1e-4),
+i.e. 2 N^2 pairwise interactions.  ``value`` is interactions per second with
+the particles resident in HBM (device-pointer entry point, CUDA events on the
+launching stream, L2 flushed between steps).  ``e2e`` is the same metric
+through the reference-facing C-ABI (``acc_kernel`` / ``acc_jerk_kernel``)
+from pinned host arrays, copies included.  The roofline line covers the
+dominant kernel, the AccJerk sweep, against the FP32 FMA throughput measured
+in the same run.  The FP64 (EXACT) path's rate is measured on an i-subset
+(the cost is exactly linear in ni) for the SPLIT / FP64 ratio.
+
+``--impl reference`` times the CPU restatement of the reference kernels
+(bit-identical to them) on all host cores over a bounded i-subset of the
+same workload.
+
+Multi-GPU (torchrun): every rank runs the same sweep on its own GPU
+(replicas; the sweep has no exchange), value = all ranks' interactions over
+the slowest rank's time.
+"""
+
+import argparse
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = ("Gint/s at N=256k FP32-split vs fp64 (same GPU, |da|/|a|<=1e-6); "
+          "Kepler solves/s")
+FLOPS_ACC = 20      # acc_kernel_common.h:38
+FLOPS_ACC_JERK = 42  # acc_jerk_kernel_common.h:56
+
+
+def parse():
+    p = argparse.ArgumentParser()
+    p.add_argument("--gpus", type=int, default=1)
+    p.add_argument("--steps", type=int, default=5)
+    p.add_argument("--warmup", type=int, default=3)
+    p.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    p.add_argument("--n", type=int, default=262144)
+    p.add_argument("--fp64-ni", type=int, default=8192)
+    p.add_argument("--cpu-ni", type=int, default=32768)
+    p.add_argument("--no-cpu", action="store_true")
+    return p.parse_args()
+
+
+def dist_env():
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return rank, world, local
+
+
+class ClockSampler(object):
+    """nvidia-smi clock/throttle samples while the timed region runs."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,"
+              "clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,"
+              "clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,"
+              "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index):
+        self.index = index
+        self.proc = None
+        self.lines = []
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.index),
+                 "--query-gpu=" + self.FIELDS, "--format=csv,noheader,nounits",
+                 "-lms", "200"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except Exception:
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown",
+                 "sw_power_cap"]
+        for ln in self.lines:
+            f = [x.strip() for x in ln.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                mx.append(float(f[2]))
+            except ValueError:
+                continue
+            for nm, v in zip(names, f[5:9]):
+                if v.lower().startswith("active"):
+                    reasons.add(nm)
+        return {"sm_mhz": float(np.median(sm)) if sm else None,
+                "sm_max_mhz": float(max(mx)) if mx else None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def roofline_traffic():
+    """dram bytes per AccJerk launch from the committed ncu summary."""
+    path = os.path.join(ROOT, "profiles", "acc_jerk_split_n262144.md")
+    try:
+        for line in open(path):
+            if line.startswith("dram_bytes_per_launch:"):
+                return float(line.split(":", 1)[1])
+    except OSError:
+        pass
+    return None
+
+
+def cpu_baseline(n, ni, ps):
+    """Oracle (bit-identical restatement of the reference C kernels) on all
+    host threads over ni i-particles x all n j-particles, both kernels."""
+    import oracle
+    threads = oracle.max_threads()
+    sub = {k: np.ascontiguousarray(v[:ni]) for k, v in ps.items()}
+    t0 = time.perf_counter()
+    oracle.run("acc_kernel", sub, ps)
+    oracle.run("acc_jerk_kernel", sub, ps)
+    dt = time.perf_counter() - t0
+    return {"value": 2.0 * ni * n / dt / 1e9, "unit": "Gint/s",
+            "cores": threads, "kind": "port",
+            "sample": "acc + acc_jerk, ni=%d x nj=%d of the N=%d Plummer "
+                      "sphere (%.1f s)" % (ni, n, n, dt)}
+
+
+def run_reference(args):
+    """--impl reference: the reference kernels' CPU path (the oracle port,
+    bit-identical to tupan's C backend) on all host threads."""
+    rank, world, local = dist_env()
+    if rank != 0:
+        return
+    from tupan_gb300 import ics
+    import oracle
+    n = args.n
+    ps = ics.plummer(n, eps=1e-4, seed=1)
+    ni = args.cpu_ni
+    sub = {k: np.ascontiguousarray(v[:ni]) for k, v in ps.items()}
+    threads = oracle.max_threads()
+    for _ in range(max(1, args.warmup) if False else 1):
+        oracle.run("acc_kernel", {k: v[:64].copy() for k, v in sub.items()}, ps)
+    times = []
+    for _ in range(args.steps):
+        t0 = time.perf_counter()
+        oracle.run("acc_kernel", sub, ps)
+        oracle.run("acc_jerk_kernel", sub, ps)
+        times.append(time.perf_counter() - t0)
+    t = float(np.mean(times))
+    val = 2.0 * ni * n / t / 1e9
+    line = {"metric": METRIC, "value": val, "unit": "Gint/s", "n_gpus": world,
+            "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": t * 1e3, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+            "data": "synthetic Plummer sphere (seeded)",
+            "config": {"workload": "acc+acc_jerk sweep, Plummer N=%d eps=1e-4"
+                                   % n, "sample_ni": ni, "n": n},
+            "impl": "reference",
+            "cpu_baseline": {"value": val, "unit": "Gint/s", "cores": threads,
+                             "kind": "port",
+                             "sample": "ni=%d x nj=%d per step" % (ni, n)},
+            "e2e": {"value": val, "unit": "Gint/s", "h2d_bytes_per_step": 0,
+                    "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    args = parse()
+    if args.impl == "reference":
+        run_reference(args)
+        return
+    rank, world, local = dist_env()
+    import torch
+    import torch.distributed as dist
+    from tupan_gb300 import ics, lib
+
+    torch.cuda.set_device(local)
+    if world > 1:
+        dist.init_process_group("nccl")
+    dev = torch.device("cuda", local)
+    n = args.n
+    ps = ics.plummer(n, eps=1e-4, seed=1 + rank)
+    names8 = ("m", "rx", "ry", "rz", "e2", "vx", "vy", "vz")
+    d_in = {k: torch.from_numpy(ps[k]).to(dev) for k in names8}
+    d_acc = [torch.empty(n, dtype=torch.float64, device=dev) for _ in range(3)]
+    d_aj = [torch.empty(n, dtype=torch.float64, device=dev) for _ in range(6)]
+    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32,
+                        device=dev)
+    stream = torch.cuda.current_stream(dev)
+    sh = stream.cuda_stream
+    p5 = [d_in[k].data_ptr() for k in names8[:5]]
+    p8 = [d_in[k].data_ptr() for k in names8]
+
+    def step(mode=lib.MODE_SPLIT, ni=n):
+        lib.dev_sweep("acc_kernel", ni, p5, n, p5,
+                      [t.data_ptr() for t in d_acc], mode=mode, stream=sh)
+        lib.dev_sweep("acc_jerk_kernel", ni, p8, n, p8,
+                      [t.data_ptr() for t in d_aj], mode=mode, stream=sh)
+
+    # --- device-resident timing (value) -----------------------------------
+    for _ in range(args.warmup):
+        step()
+    torch.cuda.synchronize()
+    launches0 = lib.load().tupan_gb300_launch_count()
+    ev = [(torch.cuda.Event(enable_timing=True),
+           torch.cuda.Event(enable_timing=True),
+           torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
+    clocks = ClockSampler(local)
+    if world > 1:
+        dist.barrier()
+    torch.cuda.synchronize()
+    clocks.start()
+    t_wall = time.perf_counter()
+    for k in range(args.steps):
+        flush.fill_(float(k))                 # evict L2 between steps
+        a, b, c = ev[k]
+        a.record(stream)
+        lib.dev_sweep("acc_kernel", n, p5, n, p5,
+                      [t.data_ptr() for t in d_acc], mode=lib.MODE_SPLIT,
+                      stream=sh)
+        b.record(stream)
+        lib.dev_sweep("acc_jerk_kernel", n, p8, n, p8,
+                      [t.data_ptr() for t in d_aj], mode=lib.MODE_SPLIT,
+                      stream=sh)
+        c.record(stream)
+    torch.cuda.synchronize()
+    t_wall = time.perf_counter() - t_wall
+    clk = clocks.stop()
+    if world > 1:
+        dist.barrier()
+    launches = lib.load().tupan_gb300_launch_count() - launches0
+    t_acc = sum(e[0].elapsed_time(e[1]) for e in ev) / 1e3 / args.steps
+    t_aj = sum(e[1].elapsed_time(e[2]) for e in ev) / 1e3 / args.steps
+    t_step = t_acc + t_aj
+    if world > 1:
+        tt = torch.tensor([t_step, t_acc, t_aj], dtype=torch.float64,
+                          device=dev)
+        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
+        t_step, t_acc, t_aj = tt.tolist()
+    inter = 2.0 * n * n
+    value = world * inter / t_step / 1e9
+
+    # accuracy of this run's AccJerk against the oracle on an i-subset
+    acc_err = None
+    if rank == 0:
+        import oracle
+        idx = np.sort(np.random.default_rng(0).choice(n, 128, replace=False))
+        sub = {k: np.ascontiguousarray(ps[k][idx]) for k in names8}
+        want = oracle.run("acc_jerk_kernel", sub, ps)
+        got = [t.cpu().numpy()[idx] for t in d_aj]
+        ga = np.stack(got[:3])
+        wa = np.stack(want[:3])
+        rel = np.linalg.norm(ga - wa, axis=0) / np.linalg.norm(wa, axis=0)
+        acc_err = {"max": float(rel.max()), "median": float(np.median(rel)),
+                   "sample_i": int(len(idx))}
+
+    # --- FP64 EXACT path on an i-subset (linear in ni) ---------------------
+    ni64 = min(args.fp64_ni, n)
+    step(lib.MODE_EXACT, ni64)     # warm
+    torch.cuda.synchronize()
+    e0, e1, e2 = (torch.cuda.Event(enable_timing=True) for _ in range(3))
+    e0.record(stream)
+    lib.dev_sweep("acc_kernel", ni64, p5, n, p5,
+                  [t.data_ptr() for t in d_acc], mode=lib.MODE_EXACT,
+                  stream=sh)
+    e1.record(stream)
+    lib.dev_sweep("acc_jerk_kernel", ni64, p8, n, p8,
+                  [t.data_ptr() for t in d_aj], mode=lib.MODE_EXACT,
+                  stream=sh)
+    e2.record(stream)
+    torch.cuda.synchronize()
+    t64 = (e0.elapsed_time(e2)) / 1e3
+    fp64_gints = 2.0 * ni64 * n / t64 / 1e9
+    fp64_aj_gints = ni64 * n / (e1.elapsed_time(e2) / 1e3) / 1e9
+
+    # --- FP32 FMA throughput measured now (roofline denominator) ----------
+    peak = lib.load()
+    import ctypes
+    peak.tupan_gb300_fp32_peak_tflops.restype = ctypes.c_double
+    peak.tupan_gb300_fp32_peak_tflops.argtypes = [ctypes.c_int, ctypes.c_int]
+    fp32_peak = float(peak.tupan_gb300_fp32_peak_tflops(20000, 5))
+
+    # --- end to end through the reference-facing C-ABI (host arrays) ------
+    pinned = {k: torch.from_numpy(ps[k]).pin_memory() for k in names8}
+    hp = {k: pinned[k].numpy() for k in names8}
+    h_acc = [torch.empty(n, dtype=torch.float64).pin_memory().numpy()
+             for _ in range(3)]
+    h_aj = [torch.empty(n, dtype=torch.float64).pin_memory().numpy()
+            for _ in range(6)]
+    from tupan_gb300 import abi
+    f_acc = lib.bind("acc_kernel")
+    f_aj = lib.bind("acc_jerk_kernel")
+    old_mode = lib.set_mode(lib.MODE_SPLIT)
+
+    def host_step():
+        va = abi.make_args("acc_kernel", "float64", hp, hp, None,
+                           {"iax": h_acc[0], "iay": h_acc[1], "iaz": h_acc[2]})
+        abi.call(f_acc, "acc_kernel", "float64", va)
+        vj = abi.make_args("acc_jerk_kernel", "float64", hp, hp, None,
+                           dict(zip(("iax", "iay", "iaz", "ijx", "ijy", "ijz"),
+                                    h_aj)))
+        abi.call(f_aj, "acc_jerk_kernel", "float64", vj)
+        lib.check()
+
+    host_step()
+    t0 = time.perf_counter()
+    ksteps = max(1, min(args.steps, 3))
+    for _ in range(ksteps):
+        host_step()
+    t_e2e = (time.perf_counter() - t0) / ksteps
+    lib.set_mode(old_mode)
+    h2d = 8 * n * (5 + 8)
+    d2h = 8 * n * (3 + 6)
+    e2e_val = world * inter / t_e2e / 1e9
+
+    if rank != 0:
+        if world > 1:
+            dist.destroy_process_group()
+        return
+    cpu = None if args.no_cpu else cpu_baseline(n, args.cpu_ni, ps)
+    achieved = n * n * FLOPS_ACC_JERK / t_aj / 1e12
+    traffic = roofline_traffic()
+    v_aj, g_aj = lib.split_choice("acc_jerk_kernel", n, n)
+    line = {
+        "metric": METRIC, "value": value, "unit": "Gint/s",
+        "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": t_step * 1e3, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32-split",
+        "data": "synthetic Plummer sphere (seeded, equal masses)",
+        "config": {"workload": "acc + acc_jerk sweep, all i vs all j, Plummer "
+                               "N=%d eps=1e-4, SPLIT mode" % n,
+                   "n": n, "interactions_per_step": inter,
+                   "l2": "flushed between steps (256 MiB write)",
+                   "parallelism": "replicas" if world > 1 else "single GPU",
+                   "acc_jerk_variant": v_aj, "acc_jerk_gsplit": g_aj},
+        "kernels": {"acc_split_gints": n * n / t_acc / 1e9,
+                    "acc_jerk_split_gints": n * n / t_aj / 1e9,
+                    "fp64_exact_gints": fp64_gints,
+                    "fp64_exact_acc_jerk_gints": fp64_aj_gints,
+                    "fp64_sample_ni": ni64,
+                    "split_over_fp64": (inter / t_step) / (2.0 * ni64 * n / t64),
+                    "acc_rel_err_vs_fp64_oracle": acc_err},
+        "roofline": {"bound": "fp32", "kernel": "split_sweep<AccJerkS>",
+                     "achieved": achieved, "peak": fp32_peak,
+                     "unit": "TFLOP/s", "frac": achieved / fp32_peak,
+                     "flops_per_interaction": FLOPS_ACC_JERK,
+                     "peak_source": "FP32 FMA-chain kernel measured in this "
+                                    "run (MEASURED_PEAKS.json has no FP32 "
+                                    "figure)",
+                     "traffic": traffic},
+        "cpu_baseline": cpu,
+        "e2e": {"value": e2e_val, "unit": "Gint/s",
+                "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
+                "path": "acc_kernel + acc_jerk_kernel C-ABI, pinned host "
+                        "arrays, SPLIT mode", "ms_per_step": t_e2e * 1e3},
+        "gpu_launches": int(launches),
+        "clocks": clk,
+        "wall_s_timed": t_wall,
+    }
+    print(json.dumps(line), flush=True)
+    if world > 1:
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,219 @@
+/*
+ * tupan_gb300.h -- C-ABI of the GB300 (sm_103a) tupan kernel layer.
+ *
+ * Two shared libraries implement it:
+ *   libtupan_gb300.so     REAL = double, UINT = uint64_t, INT = int64_t
+ *   libtupan_gb300_sp.so  REAL = float,  UINT = uint32_t, INT = int32_t
+ *                         (compile against this header with TUPAN_GB300_SP)
+ * matching the two precisions tupan builds from tupan/lib/src/libtupan.h
+ * (tupan/lib/cffi_backend.py:31-87: typedefs at :53-55, libraries at :84-87).
+ *
+ * The first ten functions replace the reference's kernels one for one: same
+ * names, same argument order and meaning, void return.  They take HOST
+ * arrays; inputs are copied to the GPU, the pairwise sums run there, results
+ * are copied back before the call returns.  Every output array is overwritten
+ * for all ni entries, as in the reference.  i and j arrays may be the same
+ * arrays.  After a call, tupan_gb300_last_error() is 0 on success.
+ */
+#ifndef TUPAN_GB300_H
+#define TUPAN_GB300_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#ifdef TUPAN_GB300_SP
+typedef float TG_REAL;
+typedef uint32_t TG_UINT;
+typedef int32_t TG_INT;
+#else
+typedef double TG_REAL;
+typedef uint64_t TG_UINT;
+typedef int64_t TG_INT;
+#endif
+
+/* Replaces phi_kernel, tupan/lib/src/libtupan.h:2-15 (phi_kernel.c:5-34). */
+void phi_kernel(const TG_UINT ni, const TG_REAL *im, const TG_REAL *irx,
+                const TG_REAL *iry, const TG_REAL *irz, const TG_REAL *ie2,
+                const TG_UINT nj, const TG_REAL *jm, const TG_REAL *jrx,
+                const TG_REAL *jry, const TG_REAL *jrz, const TG_REAL *je2,
+                TG_REAL *iphi);
+
+/* Replaces acc_kernel, libtupan.h:17-32 (acc_kernel.c:5-40). */
+void acc_kernel(const TG_UINT ni, const TG_REAL *im, const TG_REAL *irx,
+                const TG_REAL *iry, const TG_REAL *irz, const TG_REAL *ie2,
+                const TG_UINT nj, const TG_REAL *jm, const TG_REAL *jrx,
+                const TG_REAL *jry, const TG_REAL *jrz, const TG_REAL *je2,
+                TG_REAL *iax, TG_REAL *iay, TG_REAL *iaz);
+
+/* Replaces acc_jerk_kernel, libtupan.h:34-58 (acc_jerk_kernel.c:5-60). */
+void acc_jerk_kernel(const TG_UINT ni, const TG_REAL *im, const TG_REAL *irx,
+                     const TG_REAL *iry, const TG_REAL *irz,
+                     const TG_REAL *ie2, const TG_REAL *ivx,
+                     const TG_REAL *ivy, const TG_REAL *ivz, const TG_UINT nj,
+                     const TG_REAL *jm, const TG_REAL *jrx, const TG_REAL *jry,
+                     const TG_REAL *jrz, const TG_REAL *je2,
+                     const TG_REAL *jvx, const TG_REAL *jvy,
+                     const TG_REAL *jvz, TG_REAL *iax, TG_REAL *iay,
+                     TG_REAL *iaz, TG_REAL *ijx, TG_REAL *ijy, TG_REAL *ijz);
+
+/* Replaces snap_crackle_kernel, libtupan.h:60-96
+ * (snap_crackle_kernel.c:5-82). */
+void snap_crackle_kernel(
+    const TG_UINT ni, const TG_REAL *im, const TG_REAL *irx,
+    const TG_REAL *iry, const TG_REAL *irz, const TG_REAL *ie2,
+    const TG_REAL *ivx, const TG_REAL *ivy, const TG_REAL *ivz,
+    const TG_REAL *iax, const TG_REAL *iay, const TG_REAL *iaz,
+    const TG_REAL *ijx, const TG_REAL *ijy, const TG_REAL *ijz,
+    const TG_UINT nj, const TG_REAL *jm, const TG_REAL *jrx,
+    const TG_REAL *jry, const TG_REAL *jrz, const TG_REAL *je2,
+    const TG_REAL *jvx, const TG_REAL *jvy, const TG_REAL *jvz,
+    const TG_REAL *jax, const TG_REAL *jay, const TG_REAL *jaz,
+    const TG_REAL *jjx, const TG_REAL *jjy, const TG_REAL *jjz, TG_REAL *isx,
+    TG_REAL *isy, TG_REAL *isz, TG_REAL *icx, TG_REAL *icy, TG_REAL *icz);
+
+/* Replaces tstep_kernel, libtupan.h:98-119 (tstep_kernel.c:5-49). */
+void tstep_kernel(const TG_UINT ni, const TG_REAL *im, const TG_REAL *irx,
+                  const TG_REAL *iry, const TG_REAL *irz, const TG_REAL *ie2,
+                  const TG_REAL *ivx, const TG_REAL *ivy, const TG_REAL *ivz,
+                  const TG_UINT nj, const TG_REAL *jm, const TG_REAL *jrx,
+                  const TG_REAL *jry, const TG_REAL *jrz, const TG_REAL *je2,
+                  const TG_REAL *jvx, const TG_REAL *jvy, const TG_REAL *jvz,
+                  const TG_REAL eta, TG_REAL *idt_a, TG_REAL *idt_b);
+
+/* Replaces pnacc_kernel, libtupan.h:121-150 (pnacc_kernel.c:5-60). */
+void pnacc_kernel(const TG_UINT ni, const TG_REAL *im, const TG_REAL *irx,
+                  const TG_REAL *iry, const TG_REAL *irz, const TG_REAL *ie2,
+                  const TG_REAL *ivx, const TG_REAL *ivy, const TG_REAL *ivz,
+                  const TG_UINT nj, const TG_REAL *jm, const TG_REAL *jrx,
+                  const TG_REAL *jry, const TG_REAL *jrz, const TG_REAL *je2,
+                  const TG_REAL *jvx, const TG_REAL *jvy, const TG_REAL *jvz,
+                  TG_UINT order, const TG_REAL inv1, const TG_REAL inv2,
+                  const TG_REAL inv3, const TG_REAL inv4, const TG_REAL inv5,
+                  const TG_REAL inv6, const TG_REAL inv7, TG_REAL *ipnax,
+                  TG_REAL *ipnay, TG_REAL *ipnaz);
+
+/* Replaces nreg_Xkernel, libtupan.h:152-178 (nreg_kernels.c:5-67). */
+void nreg_Xkernel(const TG_UINT ni, const TG_REAL *im, const TG_REAL *irx,
+                  const TG_REAL *iry, const TG_REAL *irz, const TG_REAL *ie2,
+                  const TG_REAL *ivx, const TG_REAL *ivy, const TG_REAL *ivz,
+                  const TG_UINT nj, const TG_REAL *jm, const TG_REAL *jrx,
+                  const TG_REAL *jry, const TG_REAL *jrz, const TG_REAL *je2,
+                  const TG_REAL *jvx, const TG_REAL *jvy, const TG_REAL *jvz,
+                  const TG_REAL dt, TG_REAL *idrx, TG_REAL *idry,
+                  TG_REAL *idrz, TG_REAL *iax, TG_REAL *iay, TG_REAL *iaz,
+                  TG_REAL *iu);
+
+/* Replaces nreg_Vkernel, libtupan.h:180-201 (nreg_kernels.c:70-115). */
+void nreg_Vkernel(const TG_UINT ni, const TG_REAL *im, const TG_REAL *ivx,
+                  const TG_REAL *ivy, const TG_REAL *ivz, const TG_REAL *iax,
+                  const TG_REAL *iay, const TG_REAL *iaz, const TG_UINT nj,
+                  const TG_REAL *jm, const TG_REAL *jvx, const TG_REAL *jvy,
+                  const TG_REAL *jvz, const TG_REAL *jax, const TG_REAL *jay,
+                  const TG_REAL *jaz, const TG_REAL dt, TG_REAL *idvx,
+                  TG_REAL *idvy, TG_REAL *idvz, TG_REAL *ik);
+
+/* Replaces sakura_kernel, libtupan.h:203-229 (sakura_kernel.c:5-63). */
+void sakura_kernel(const TG_UINT ni, const TG_REAL *im, const TG_REAL *irx,
+                   const TG_REAL *iry, const TG_REAL *irz,
+                   const TG_REAL *ie2, const TG_REAL *ivx, const TG_REAL *ivy,
+                   const TG_REAL *ivz, const TG_UINT nj, const TG_REAL *jm,
+                   const TG_REAL *jrx, const TG_REAL *jry, const TG_REAL *jrz,
+                   const TG_REAL *je2, const TG_REAL *jvx, const TG_REAL *jvy,
+                   const TG_REAL *jvz, const TG_REAL dt, const TG_INT flag,
+                   TG_REAL *idrx, TG_REAL *idry, TG_REAL *idrz,
+                   TG_REAL *idvx, TG_REAL *idvy, TG_REAL *idvz);
+
+/* Replaces kepler_solver_kernel, libtupan.h:231-246
+ * (kepler_solver_kernel.c:5-49).  Two particles; outputs may alias inputs. */
+void kepler_solver_kernel(const TG_REAL *im, const TG_REAL *irx,
+                          const TG_REAL *iry, const TG_REAL *irz,
+                          const TG_REAL *ie2, const TG_REAL *ivx,
+                          const TG_REAL *ivy, const TG_REAL *ivz,
+                          const TG_REAL dt, TG_REAL *ir1x, TG_REAL *ir1y,
+                          TG_REAL *ir1z, TG_REAL *iv1x, TG_REAL *iv1y,
+                          TG_REAL *iv1z);
+
+/* ------------------------------------------------------------------------
+ * Extensions (no counterpart in the reference, whose kernels return void
+ * and cannot fail, tupan/lib/src/libtupan.h:2-246).
+ * ---------------------------------------------------------------------- */
+
+/* Kernel ids used by the extension calls, in libtupan.h order. */
+enum {
+    TUPAN_GB300_PHI = 0, TUPAN_GB300_ACC = 1, TUPAN_GB300_ACC_JERK = 2,
+    TUPAN_GB300_SNAP_CRACKLE = 3, TUPAN_GB300_TSTEP = 4,
+    TUPAN_GB300_PNACC = 5, TUPAN_GB300_NREG_X = 6, TUPAN_GB300_NREG_V = 7,
+    TUPAN_GB300_SAKURA = 8, TUPAN_GB300_KEPLER = 9
+};
+
+/* Status of the last call (0 = success; 1 CUDA error, 2 bad argument,
+ * 3 device error word set, 4 no device, 5 request too large) and its text. */
+int tupan_gb300_last_error(void);
+const char *tupan_gb300_last_error_message(void);
+/* Device error word of the last sweep: bit 0 copy-pipeline wait ran out,
+ * bit 1 a Kepler solve exceeded its solve budget. */
+unsigned tupan_gb300_last_device_error(void);
+
+/* Arithmetic mode: 0 EXACT (default; bit-identical to the reference C for all
+ * kernels but Sakura/Kepler, which agree to libm accuracy), 1 SPLIT (FP32
+ * pairs on double-single positions with compensated sums; float64 library,
+ * kernels phi/acc/acc_jerk/snap_crackle/tstep -- the others stay EXACT).
+ * Returns the previous mode.  The environment variable TUPAN_GB300_MODE=split
+ * selects SPLIT at load time. */
+int tupan_gb300_set_mode(int mode);
+int tupan_gb300_get_mode(void);
+
+/* Bound on single-step solves per Kepler pair solve (default 2^20); the
+ * reference's retry loops have none. Returns the previous bound. */
+long long tupan_gb300_set_kepler_budget(long long budget);
+
+/* SPLIT-mode launch configuration: variant in [0, tupan_gb300_split_variants())
+ * and grid j-split count; set_split_config forces it for a kernel
+ * (variant < 0 restores the automatic choice), set_tuned records it for sizes
+ * in the same power-of-two buckets, split_choice reports the choice. */
+int tupan_gb300_set_split_config(int kernel, int variant, int gsplit);
+int tupan_gb300_set_tuned(int kernel, uint64_t ni, uint64_t nj, int variant,
+                          int gsplit);
+int tupan_gb300_split_choice(int kernel, uint64_t ni, uint64_t nj,
+                             int *variant, int *gsplit);
+int tupan_gb300_split_variants(void);
+void tupan_gb300_split_variant_info(int variant, int *ni_per_thread,
+                                    int *jsplit, int *threads);
+
+/* One sweep over DEVICE arrays.  i_attrs / j_attrs: host arrays holding the
+ * device pointers of the kernel's per-particle inputs in libtupan.h order
+ * (j_attrs unused for Kepler); outs: device pointers of its outputs.
+ * scal[0] = eta (tstep) or dt (nreg, sakura, kepler); scal[1..7] = 1/c^k
+ * (pnacc).  iscal = flag (sakura) or PN order (pnacc).  mode < 0 uses the
+ * library mode.  stream may be NULL.  Asynchronous unless sync != 0.
+ * Returns a status code. */
+int tupan_gb300_dev_sweep(int kernel, int mode, uint64_t ni,
+                          const void *const *i_attrs, uint64_t nj,
+                          const void *const *j_attrs, const double *scal,
+                          int64_t iscal, void *const *outs, void *stream,
+                          int sync);
+
+/* Inputs per particle and outputs of a kernel id. */
+int tupan_gb300_kernel_arity(int kernel, int *n_inputs, int *n_outputs);
+/* Streaming multiprocessors of the current device (0 without one). */
+int tupan_gb300_device_sms(void);
+/* 64 for libtupan_gb300.so, 32 for libtupan_gb300_sp.so. */
+int tupan_gb300_real_bits(void);
+/* Kernels launched by this library since it was loaded. */
+unsigned long long tupan_gb300_launch_count(void);
+
+/* FP32 FMA throughput probe: tupan_gb300_fma_sweep launches independent FMA
+ * chains on every SM on `stream` and returns the flops it performs (for
+ * timing by the caller); tupan_gb300_fp32_peak_tflops times `reps` sweeps
+ * itself and returns the best TFLOP/s. */
+double tupan_gb300_fma_sweep(int iters, void *stream);
+double tupan_gb300_fp32_peak_tflops(int iters, int reps);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* TUPAN_GB300_H */

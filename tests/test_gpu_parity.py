@@ -1,0 +1,316 @@
+"""GPU parity of the CUDA library against the reference and the oracle.
+
+All calls go through the C-ABI (ctypes on libtupan_gb300{,_sp}.so).
+
+* EXACT mode: bit-identical to the reference's own outputs (golden fixtures)
+  and to the oracle on edge sizes and j-prefix sweeps, for every kernel but
+  Sakura/Kepler; those agree within the stated tolerance (CUDA's
+  cos/sin/cosh/sinh/log versus the host libm).
+* SPLIT mode: max |da|/|a| <= 1e-6 per particle against the fp64 oracle on
+  Plummer spheres, plus the other outputs with their stated bounds.
+"""
+
+import numpy as np
+import pytest
+
+import oracle
+from tests import golden_cases
+from tupan_gb300 import abi, ics, lib
+
+pytestmark = pytest.mark.gpu
+
+TRANSCENDENTAL = ("sakura_kernel", "kepler_solver_kernel")
+
+
+def run_gpu(name, ips, jps=None, scalars=None, prec="float64", mode=None):
+    fn = lib.bind(name, prec)
+    vals = abi.make_args(name, prec, ips, jps, scalars)
+    old = None
+    if mode is not None and prec == "float64":
+        old = lib.set_mode(mode)
+    try:
+        abi.call(fn, name, prec, vals)
+        lib.check(prec)
+    finally:
+        if old is not None:
+            lib.set_mode(old)
+    return abi.outputs(name, vals)
+
+
+def close_enough(got, want, rtol, floor=1e-3):
+    """|g - w| <= rtol * max(|w|, floor * max|w|) element-wise."""
+    scale = np.maximum(np.abs(want), floor * np.abs(want).max() + 1e-300)
+    return np.all(np.abs(got - want) <= rtol * scale)
+
+
+# ---------------------------------------------------------------------------
+# EXACT mode against the reference's golden outputs
+# ---------------------------------------------------------------------------
+def _golden():
+    for path in golden_cases.files():
+        prec, data, cases, kepler = golden_cases.load(path)
+        for (tag, name, ips, jps, scalars, expect) in cases:
+            yield pytest.param(prec, name, ips, jps, scalars, expect,
+                               id="%s:%s" % (path.rsplit("/", 1)[1], tag))
+
+
+@pytest.mark.parametrize("prec,name,ips,jps,scalars,expect", list(_golden()))
+def test_exact_matches_reference_golden(prec, name, ips, jps, scalars, expect):
+    got = run_gpu(name, ips, jps, scalars, prec, mode=lib.MODE_EXACT)
+    for g, e in zip(got, expect):
+        if name in TRANSCENDENTAL:
+            rtol = 1e-9 if prec == "float64" else 2e-3
+            assert close_enough(g, e, rtol), (name, np.abs(g - e).max())
+        else:
+            np.testing.assert_array_equal(g, e)
+
+
+def _golden_kepler():
+    for path in golden_cases.files():
+        prec, data, cases, kepler = golden_cases.load(path)
+        for (dt, pairs, res) in kepler:
+            yield pytest.param(prec, data, dt, pairs, res,
+                               id="%s:dt=%r" % (path.rsplit("/", 1)[1], dt))
+
+
+@pytest.mark.parametrize("prec,data,dt,pairs,res", list(_golden_kepler()))
+def test_exact_kepler_matches_reference_golden(prec, data, dt, pairs, res):
+    for row, p in enumerate(pairs):
+        two = {a: np.ascontiguousarray(v[2 * p:2 * p + 2])
+               for a, v in data.items()}
+        got = np.concatenate(run_gpu("kepler_solver_kernel", two, None,
+                                     {"dt": dt}, prec))
+        rtol = 1e-10 if prec == "float64" else 1e-3
+        scale = np.abs(res[row]).max()
+        assert np.max(np.abs(got - res[row])) <= rtol * scale, (p, dt)
+
+
+# ---------------------------------------------------------------------------
+# EXACT mode against the oracle: edge sizes, j-prefix sweeps, both roles
+# ---------------------------------------------------------------------------
+SCALARS = {
+    "tstep_kernel": {"eta": 1.0 / 64},
+    "pnacc_kernel": dict(order=7, **{"inv%d" % k: (1.0 / 128) ** k
+                                     for k in range(1, 8)}),
+    "nreg_Xkernel": {"dt": 1.0 / 64},
+    "nreg_Vkernel": {"dt": 1.0 / 64},
+    "sakura_kernel": {"dt": 1.0 / 64, "flag": 1},
+}
+SWEEP_KERNELS = [k for k in abi.KERNEL_NAMES if k != "kepler_solver_kernel"]
+
+
+def uniform(n, seed, prec="float64", eps2=0.0):
+    rng = np.random.default_rng(seed)
+    dt = abi.numpy_real(prec)
+    d = {"m": rng.random(n), "e2": np.full(n, eps2)}
+    for k in ("rx", "ry", "rz", "vx", "vy", "vz"):
+        d[k] = rng.random(n) * 10
+    for k in ("ax", "ay", "az", "jx", "jy", "jz"):
+        d[k] = rng.standard_normal(n)
+    return {k: np.ascontiguousarray(v, dtype=dt) for k, v in d.items()}
+
+
+EDGE_SIZES = [(1, 1), (1, 300), (300, 1), (2, 3), (31, 33), (257, 129),
+              (129, 257), (1000, 1000)]
+
+
+@pytest.mark.parametrize("prec", ["float64", "float32"])
+@pytest.mark.parametrize("name", SWEEP_KERNELS)
+@pytest.mark.parametrize("ni,nj", EDGE_SIZES)
+def test_exact_edge_sizes(prec, name, ni, nj):
+    ips = uniform(ni, 11 + ni, prec, eps2=1e-4 if ni % 2 else 0.0)
+    jps = uniform(nj, 17 + nj, prec, eps2=1e-4 if ni % 2 else 0.0)
+    sc = SCALARS.get(name, {})
+    got = run_gpu(name, ips, jps, sc, prec, mode=lib.MODE_EXACT)
+    want = oracle.run(name, ips, jps, sc, prec)
+    for g, w in zip(got, want):
+        if name in TRANSCENDENTAL:
+            assert close_enough(g, w, 1e-9 if prec == "float64" else 2e-3)
+        else:
+            np.testing.assert_array_equal(g, w)
+
+
+@pytest.mark.parametrize("name", SWEEP_KERNELS)
+def test_exact_self_interaction_and_aliasing(name):
+    # ips and jps are the same arrays (tupan's ps.set_acc(ps)); the r2 > 0
+    # mask must drop the self pairs exactly as in the reference.
+    ps = uniform(200, 5)
+    sc = SCALARS.get(name, {})
+    got = run_gpu(name, ps, ps, sc, mode=lib.MODE_EXACT)
+    want = oracle.run(name, ps, ps, sc)
+    for g, w in zip(got, want):
+        if name in TRANSCENDENTAL:
+            assert close_enough(g, w, 1e-9)
+        else:
+            np.testing.assert_array_equal(g, w)
+
+
+@pytest.mark.parametrize("name", ["acc_jerk_kernel", "tstep_kernel",
+                                  "snap_crackle_kernel", "pnacc_kernel"])
+def test_exact_jprefix_sweep_both_roles(name):
+    # tupan/tests/test_extensions.py:45-85: every j-prefix, both roles.
+    ps = uniform(96, 3)
+    sc = SCALARS.get(name, {})
+    for jdx in list(range(1, 40)) + [63, 64, 65, 95, 96]:
+        js = {k: np.ascontiguousarray(v[:jdx]) for k, v in ps.items()}
+        for (I, J) in ((ps, js), (js, ps)):
+            got = run_gpu(name, I, J, sc, mode=lib.MODE_EXACT)
+            want = oracle.run(name, I, J, sc)
+            for g, w in zip(got, want):
+                np.testing.assert_array_equal(g, w)
+
+
+@pytest.mark.parametrize("flag", [-2, -1, 0, 1, 2])
+def test_exact_sakura_flags_plummer(flag):
+    ps = ics.plummer(512, eps=0.0, seed=21, masses="salpeter")
+    sc = {"dt": 1.0 / 512, "flag": flag}
+    got = run_gpu("sakura_kernel", ps, ps, sc, mode=lib.MODE_EXACT)
+    want = oracle.run("sakura_kernel", ps, ps, sc)
+    for g, w in zip(got, want):
+        assert close_enough(g, w, 1e-9), np.abs(g - w).max()
+
+
+def test_pn_orders():
+    ps = uniform(150, 8)
+    for order in range(0, 8):
+        sc = dict(SCALARS["pnacc_kernel"], order=order)
+        got = run_gpu("pnacc_kernel", ps, ps, sc, mode=lib.MODE_EXACT)
+        want = oracle.run("pnacc_kernel", ps, ps, sc)
+        for g, w in zip(got, want):
+            np.testing.assert_array_equal(g, w)
+
+
+# ---------------------------------------------------------------------------
+# SPLIT mode accuracy (FP32 pairs, double-single positions)
+# ---------------------------------------------------------------------------
+def vec_rel_err(got, want, comps):
+    g = np.stack([got[c] for c in comps])
+    w = np.stack([want[c] for c in comps])
+    return np.linalg.norm(g - w, axis=0) / np.linalg.norm(w, axis=0)
+
+
+@pytest.mark.parametrize("n", [1000, 4096, 16384])
+def test_split_acc_accuracy(n):
+    ps = ics.plummer(n, eps=1e-4, seed=n)
+    want = oracle.run("acc_kernel", ps, ps)
+    got = run_gpu("acc_kernel", ps, ps, mode=lib.MODE_SPLIT)
+    err = vec_rel_err(got, want, (0, 1, 2))
+    assert err.max() <= 1e-6, (err.max(), np.median(err))
+
+
+@pytest.mark.parametrize("n", [1000, 4096, 16384])
+def test_split_acc_jerk_accuracy(n):
+    ps = ics.plummer(n, eps=1e-4, seed=n + 1)
+    want = oracle.run("acc_jerk_kernel", ps, ps)
+    got = run_gpu("acc_jerk_kernel", ps, ps, mode=lib.MODE_SPLIT)
+    ea = vec_rel_err(got, want, (0, 1, 2))
+    ej = vec_rel_err(got, want, (3, 4, 5))
+    assert ea.max() <= 1e-6, (ea.max(), np.median(ea))
+    assert np.median(ej) <= 1e-6 and ej.max() <= 1e-4, (ej.max(),
+                                                         np.median(ej))
+
+
+def test_split_phi_tstep_snap_accuracy():
+    n = 4096
+    ps = ics.plummer(n, eps=1e-4, seed=99)
+    aj = oracle.run("acc_jerk_kernel", ps, ps)
+    for c, k in zip(("ax", "ay", "az", "jx", "jy", "jz"), aj):
+        ps[c] = k
+    phi_w = oracle.run("phi_kernel", ps, ps)[0]
+    phi_g = run_gpu("phi_kernel", ps, ps, mode=lib.MODE_SPLIT)[0]
+    assert np.max(np.abs(phi_g - phi_w) / np.abs(phi_w)) <= 1e-6
+    sc = {"eta": 1.0 / 64}
+    ts_w = oracle.run("tstep_kernel", ps, ps, sc)
+    ts_g = run_gpu("tstep_kernel", ps, ps, sc, mode=lib.MODE_SPLIT)
+    for g, w in zip(ts_g, ts_w):
+        assert np.max(np.abs(g - w) / w) <= 1e-5
+    sn_w = oracle.run("snap_crackle_kernel", ps, ps)
+    sn_g = run_gpu("snap_crackle_kernel", ps, ps, mode=lib.MODE_SPLIT)
+    es = vec_rel_err(sn_g, sn_w, (0, 1, 2))
+    ec = vec_rel_err(sn_g, sn_w, (3, 4, 5))
+    assert np.median(es) <= 1e-5 and np.median(ec) <= 1e-5, (
+        np.median(es), np.median(ec))
+
+
+@pytest.mark.parametrize("variant", range(5))
+@pytest.mark.parametrize("gsplit", [1, 3, 8])
+def test_split_every_variant(variant, gsplit):
+    ps = ics.plummer(3000, eps=1e-4, seed=5)
+    js = {k: np.ascontiguousarray(v[:2500]) for k, v in ps.items()}
+    want = oracle.run("acc_jerk_kernel", ps, js)
+    lib.set_split_config("acc_jerk_kernel", variant, gsplit)
+    try:
+        got = run_gpu("acc_jerk_kernel", ps, js, mode=lib.MODE_SPLIT)
+    finally:
+        lib.set_split_config("acc_jerk_kernel", -1, 0)
+    ea = vec_rel_err(got, want, (0, 1, 2))
+    assert ea.max() <= 1e-6, ea.max()
+
+
+@pytest.mark.parametrize("ni,nj", [(1, 1), (1, 5000), (5000, 1), (7, 300),
+                                   (513, 257)])
+def test_split_edge_sizes(ni, nj):
+    ps = ics.plummer(max(ni, nj), eps=1e-4, seed=ni * 7 + nj)
+    ip = {k: np.ascontiguousarray(v[:ni]) for k, v in ps.items()}
+    jp = {k: np.ascontiguousarray(v[-nj:]) for k, v in ps.items()}
+    for name in ("acc_kernel", "acc_jerk_kernel", "phi_kernel"):
+        want = oracle.run(name, ip, jp)
+        got = run_gpu(name, ip, jp, mode=lib.MODE_SPLIT)
+        for g, w in zip(got, want):
+            scale = np.abs(w).max() + 1e-300
+            assert np.max(np.abs(g - w)) <= 1e-5 * scale, name
+
+
+def test_split_unsoftened_self_pairs():
+    # eps2 = 0: the r2 > 0 mask must remove self pairs without NaN.
+    ps = uniform(777, 42)
+    got = run_gpu("acc_jerk_kernel", ps, ps, mode=lib.MODE_SPLIT)
+    want = oracle.run("acc_jerk_kernel", ps, ps)
+    assert all(np.all(np.isfinite(g)) for g in got)
+    assert vec_rel_err(got, want, (0, 1, 2)).max() <= 1e-5
+
+
+def test_split_full_size_properties():
+    # N = 262144: momentum balance sum_i m_i a_i = 0 and a random i-subset
+    # checked against the oracle (exactly linear in ni).
+    n = 262144
+    ps = ics.plummer(n, eps=1e-4, seed=2024)
+    got = run_gpu("acc_jerk_kernel", ps, ps, mode=lib.MODE_SPLIT)
+    m = ps["m"]
+    for c in range(3):
+        tot = np.sum(m * got[c])
+        assert abs(tot) <= 1e-6 * np.sum(m * np.abs(got[c]))
+    rng = np.random.default_rng(0)
+    idx = np.sort(rng.choice(n, 256, replace=False))
+    sub = {k: np.ascontiguousarray(v[idx]) for k, v in ps.items()}
+    want = oracle.run("acc_jerk_kernel", sub, ps)
+    gsub = tuple(g[idx] for g in got)
+    ea = vec_rel_err(gsub, want, (0, 1, 2))
+    assert ea.max() <= 1e-6, (ea.max(), np.median(ea))
+
+
+# ---------------------------------------------------------------------------
+# Failure reporting without faulting the GPU
+# ---------------------------------------------------------------------------
+def test_kepler_budget_exhaustion_is_reported():
+    # A softened, eccentric pair over a long step: the reference's energy
+    # check never passes and it loops forever; here the bounded solver stops,
+    # flags DERR_KEPLER_BUDGET and the context stays usable.
+    two = {"m": np.array([0.006, 0.004]), "e2": np.array([1e-8, 1e-8]),
+           "rx": np.array([0.01, -0.015]), "ry": np.zeros(2),
+           "rz": np.zeros(2), "vx": np.zeros(2),
+           "vy": np.array([0.2, -0.3]), "vz": np.zeros(2)}
+    old = lib.set_kepler_budget(2000)
+    try:
+        fn = lib.bind("kepler_solver_kernel")
+        vals = abi.make_args("kepler_solver_kernel", "float64", two, None,
+                             {"dt": 37.5})
+        abi.call(fn, "kepler_solver_kernel", "float64", vals)
+        L = lib.load()
+        assert L.tupan_gb300_last_error() == 3
+        assert L.tupan_gb300_last_device_error() & lib.DERR_KEPLER_BUDGET
+    finally:
+        lib.set_kepler_budget(old)
+    ps = uniform(64, 1)
+    got = run_gpu("phi_kernel", ps, ps, mode=lib.MODE_EXACT)
+    np.testing.assert_array_equal(got[0], oracle.run("phi_kernel", ps, ps)[0])

@@ -1,0 +1,555 @@
+// SPLIT-mode sweeps: FP32 pair arithmetic on double-single positions with
+// compensated accumulation, for inputs and outputs in double.
+//
+//  * Positions are split once per call into hi + lo floats (pack kernel), so
+//    x_j - x_i is formed as (xh_j - xh_i) + (xl_j - xl_i): the difference of
+//    two nearby positions keeps ~48 bits instead of FP32's 24.
+//  * 1/sqrt(r^2 + eps^2) is rsqrt (MUFU) plus one Newton step.
+//  * Each lane sums a run of pair terms in FP32, then folds the run into a
+//    Kahan-compensated (sum, correction) pair; the final value is formed in
+//    double.  j-split lanes of one i are combined with warp shuffles, grid
+//    j-splits through a partial-sum buffer reduced in a fixed order.
+//  * j-records are staged into shared memory by bulk asynchronous copies
+//    (TMA, cp.async.bulk) into a two-stage ring guarded by mbarriers; i-data
+//    stay in registers.
+//
+// The j - i sign convention is used throughout (the reference forms i - j
+// and subtracts); every output is the same quantity.
+
+#include "tg_common.cuh"
+#include "tg_tma.cuh"
+
+namespace tg {
+
+// ---------------------------------------------------------------------------
+// Packed FP32 particle records (float4 units):
+//   [0] = {xh, yh, zh, m}   [1] = {xl, yl, zl, e2}   [2] = {vx, vy, vz, 0}
+//   [3] = {ax, ay, az, jx}  [4] = {jy, jz, 0, 0}
+// ---------------------------------------------------------------------------
+__host__ __device__ constexpr int split_nf(int k)
+{
+    return (k == K_PHI || k == K_ACC) ? 2 : (k == K_SNAP_CRACKLE ? 5 : 3);
+}
+
+struct PackArgs {
+    const double *a[MAX_ATTR];
+    int na;      // attributes present (5, 8 or 14)
+    int nf;      // float4 per record
+};
+
+__device__ __forceinline__ void split2(double x, float &h, float &l)
+{
+    h = __double2float_rn(x);
+    l = __double2float_rn(x - (double)h);
+}
+
+__global__ void pack_records(const PackArgs p, uint64_t n, float4 *out)
+{
+    for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n;
+         i += (uint64_t)gridDim.x * blockDim.x) {
+        float xh, xl, yh, yl, zh, zl;
+        split2(p.a[1][i], xh, xl);
+        split2(p.a[2][i], yh, yl);
+        split2(p.a[3][i], zh, zl);
+        float4 *r = out + i * p.nf;
+        r[0] = make_float4(xh, yh, zh, (float)p.a[0][i]);
+        r[1] = make_float4(xl, yl, zl, (float)p.a[4][i]);
+        if (p.nf >= 3)
+            r[2] = make_float4((float)p.a[5][i], (float)p.a[6][i],
+                               (float)p.a[7][i], 0.f);
+        if (p.nf >= 5) {
+            r[3] = make_float4((float)p.a[8][i], (float)p.a[9][i],
+                               (float)p.a[10][i], (float)p.a[11][i]);
+            r[4] = make_float4((float)p.a[12][i], (float)p.a[13][i], 0.f, 0.f);
+        }
+    }
+}
+
+cudaError_t launch_pack(int kernel, uint64_t n, const void *const *attrs,
+                        float4 *out, cudaStream_t st)
+{
+    if (n == 0) return cudaSuccess;
+    PackArgs p;
+    p.na = n_attr(kernel);
+    p.nf = split_nf(kernel);
+    for (int a = 0; a < MAX_ATTR; ++a)
+        p.a[a] = a < p.na ? (const double *)attrs[a] : nullptr;
+    uint64_t blocks = (n + 255) / 256;
+    if (blocks > 152 * 16) blocks = 152 * 16;
+    pack_records<<<(unsigned)blocks, 256, 0, st>>>(p, n, out);
+    g_launch_count += 1;
+    return cudaGetLastError();
+}
+
+// ---------------------------------------------------------------------------
+// Pair operators.  Each has:
+//   NF   float4 per record, NO outputs, MAXC index of a max-reduced output
+//   (or -1), I/J  register images of an i / j record, pair() accumulating
+//   into float acc[NO], finish() in double on the reduced result.
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ float rsqrt_nr(float s)
+{
+    // MUFU approximation refined by one Newton-Raphson step:
+    //   y1 = y0 (3 - s y0^2) / 2
+    float y = rsqrtf(s);
+    float t = s * y;
+    float e = fmaf(-t, y, 1.0f);
+    return fmaf(0.5f * y, e, y);
+}
+
+struct PhiS {
+    static constexpr int NF = 2, NO = 1, MAXC = -1;
+    struct P { float xh, yh, zh, m, xl, yl, zl, e2; };
+    __device__ static P load(const float4 *r)
+    {
+        float4 a = r[0], b = r[1];
+        return {a.x, a.y, a.z, a.w, b.x, b.y, b.z, b.w};
+    }
+    __device__ static void pair(const P &i, const P &j, float *acc, float)
+    {
+        float dx = (j.xh - i.xh) + (j.xl - i.xl);
+        float dy = (j.yh - i.yh) + (j.yl - i.yl);
+        float dz = (j.zh - i.zh) + (j.zl - i.zl);
+        float h2 = i.e2 + j.e2;
+        float s = fmaf(dz, dz, fmaf(dy, dy, fmaf(dx, dx, h2)));
+        float y = rsqrt_nr(s);
+        y = (s > h2) ? y : 0.0f;
+        acc[0] = fmaf(-j.m, y, acc[0]);
+    }
+    __device__ static void finish(double *, double) {}
+};
+
+struct AccS {
+    static constexpr int NF = 2, NO = 3, MAXC = -1;
+    using P = PhiS::P;
+    __device__ static P load(const float4 *r) { return PhiS::load(r); }
+    __device__ static void pair(const P &i, const P &j, float *acc, float)
+    {
+        float dx = (j.xh - i.xh) + (j.xl - i.xl);
+        float dy = (j.yh - i.yh) + (j.yl - i.yl);
+        float dz = (j.zh - i.zh) + (j.zl - i.zl);
+        float h2 = i.e2 + j.e2;
+        float s = fmaf(dz, dz, fmaf(dy, dy, fmaf(dx, dx, h2)));
+        float y = rsqrt_nr(s);
+        y = (s > h2) ? y : 0.0f;
+        float mk = (j.m * y) * (y * y);
+        acc[0] = fmaf(mk, dx, acc[0]);
+        acc[1] = fmaf(mk, dy, acc[1]);
+        acc[2] = fmaf(mk, dz, acc[2]);
+    }
+    __device__ static void finish(double *, double) {}
+};
+
+struct AccJerkS {
+    static constexpr int NF = 3, NO = 6, MAXC = -1;
+    struct P { float xh, yh, zh, m, xl, yl, zl, e2, vx, vy, vz; };
+    __device__ static P load(const float4 *r)
+    {
+        float4 a = r[0], b = r[1], c = r[2];
+        return {a.x, a.y, a.z, a.w, b.x, b.y, b.z, b.w, c.x, c.y, c.z};
+    }
+    __device__ static void pair(const P &i, const P &j, float *acc, float)
+    {
+        float dx = (j.xh - i.xh) + (j.xl - i.xl);
+        float dy = (j.yh - i.yh) + (j.yl - i.yl);
+        float dz = (j.zh - i.zh) + (j.zl - i.zl);
+        float ux = j.vx - i.vx, uy = j.vy - i.vy, uz = j.vz - i.vz;
+        float h2 = i.e2 + j.e2;
+        float s = fmaf(dz, dz, fmaf(dy, dy, fmaf(dx, dx, h2)));
+        float rv = fmaf(dz, uz, fmaf(dy, uy, dx * ux));
+        float y = rsqrt_nr(s);
+        y = (s > h2) ? y : 0.0f;
+        float y2 = y * y;
+        float mk = (j.m * y) * y2;
+        float al = (3.0f * rv) * y2;
+        acc[0] = fmaf(mk, dx, acc[0]);
+        acc[1] = fmaf(mk, dy, acc[1]);
+        acc[2] = fmaf(mk, dz, acc[2]);
+        acc[3] = fmaf(mk, fmaf(-al, dx, ux), acc[3]);
+        acc[4] = fmaf(mk, fmaf(-al, dy, uy), acc[4]);
+        acc[5] = fmaf(mk, fmaf(-al, dz, uz), acc[5]);
+    }
+    __device__ static void finish(double *, double) {}
+};
+
+// tstep_kernel_common.h:7-60 in FP32; output 0 sums w2, output 1 is max w2.
+struct TstepS {
+    static constexpr int NF = 3, NO = 2, MAXC = 1;
+    using P = AccJerkS::P;
+    __device__ static P load(const float4 *r) { return AccJerkS::load(r); }
+    __device__ static void pair(const P &i, const P &j, float *acc, float eta)
+    {
+        float dx = (j.xh - i.xh) + (j.xl - i.xl);
+        float dy = (j.yh - i.yh) + (j.yl - i.yl);
+        float dz = (j.zh - i.zh) + (j.zl - i.zl);
+        float ux = j.vx - i.vx, uy = j.vy - i.vy, uz = j.vz - i.vz;
+        float h2 = i.e2 + j.e2;
+        float msum = i.m + j.m;
+        float s = fmaf(dz, dz, fmaf(dy, dy, fmaf(dx, dx, h2)));
+        float rv = fmaf(dz, uz, fmaf(dy, uy, dx * ux));
+        float v2 = fmaf(uz, uz, fmaf(uy, uy, ux * ux));
+        float y = rsqrt_nr(s);
+        float q = y * y;
+        float phi = msum * y;
+        float w2 = q * fmaf(2.0f, phi, v2);
+        float g = q * fmaf(2.0f * q, phi, w2);
+        g *= eta * rsqrt_nr(w2);
+        w2 = fmaf(-g, rv, w2);
+        w2 = (s > h2) ? w2 : 0.0f;
+        acc[0] += w2;
+        acc[1] = fmaxf(w2, acc[1]);
+    }
+    __device__ static void finish(double *v, double eta)
+    {
+        v[0] = eta / sqrt(1.0 + v[0]);
+        v[1] = eta / sqrt(1.0 + v[1]);
+    }
+};
+
+// snap_crackle_kernel_common.h:7-95 in FP32 (all differences j - i).
+struct SnapS {
+    static constexpr int NF = 5, NO = 6, MAXC = -1;
+    struct P {
+        float xh, yh, zh, m, xl, yl, zl, e2, vx, vy, vz, ax, ay, az, jx, jy,
+            jz;
+    };
+    __device__ static P load(const float4 *r)
+    {
+        float4 a = r[0], b = r[1], c = r[2], d = r[3], e = r[4];
+        return {a.x, a.y, a.z, a.w, b.x, b.y, b.z, b.w, c.x,
+                c.y, c.z, d.x, d.y, d.z, d.w, e.x, e.y};
+    }
+    __device__ static void pair(const P &i, const P &j, float *acc, float)
+    {
+        float dx = (j.xh - i.xh) + (j.xl - i.xl);
+        float dy = (j.yh - i.yh) + (j.yl - i.yl);
+        float dz = (j.zh - i.zh) + (j.zl - i.zl);
+        float ux = j.vx - i.vx, uy = j.vy - i.vy, uz = j.vz - i.vz;
+        float Ax = j.ax - i.ax, Ay = j.ay - i.ay, Az = j.az - i.az;
+        float Jx = j.jx - i.jx, Jy = j.jy - i.jy, Jz = j.jz - i.jz;
+        float h2 = i.e2 + j.e2;
+        float s = fmaf(dz, dz, fmaf(dy, dy, fmaf(dx, dx, h2)));
+        float rv = fmaf(dz, uz, fmaf(dy, uy, dx * ux));
+        float v2 = fmaf(uz, uz, fmaf(uy, uy, ux * ux));
+        float rJ = fmaf(dz, Jz, fmaf(dy, Jy, dx * Jx));
+        float rA = fmaf(dz, Az, fmaf(dy, Ay, dx * Ax));
+        float vA = fmaf(uz, Az, fmaf(uy, Ay, ux * Ax));
+        float y = rsqrt_nr(s);
+        y = (s > h2) ? y : 0.0f;
+        float q = y * y;
+        float al = rv * q;
+        float al2 = al * al;
+        float be = 3.0f * fmaf(v2 + rA, q, al2);
+        float ga = fmaf(fmaf(3.0f, vA, rJ), q, al * fmaf(-4.0f, al2, be));
+        al *= 3.0f;
+        ga *= 3.0f;
+        ux = fmaf(-al, dx, ux);
+        uy = fmaf(-al, dy, uy);
+        uz = fmaf(-al, dz, uz);
+        float two_al = 2.0f * al;
+        Ax -= fmaf(two_al, ux, be * dx);
+        Ay -= fmaf(two_al, uy, be * dy);
+        Az -= fmaf(two_al, uz, be * dz);
+        al *= 3.0f;
+        be *= 3.0f;
+        Jx -= fmaf(al, Ax, fmaf(be, ux, ga * dx));
+        Jy -= fmaf(al, Ay, fmaf(be, uy, ga * dy));
+        Jz -= fmaf(al, Az, fmaf(be, uz, ga * dz));
+        float mk = (j.m * y) * q;
+        acc[0] = fmaf(mk, Ax, acc[0]);
+        acc[1] = fmaf(mk, Ay, acc[1]);
+        acc[2] = fmaf(mk, Az, acc[2]);
+        acc[3] = fmaf(mk, Jx, acc[3]);
+        acc[4] = fmaf(mk, Jy, acc[4]);
+        acc[5] = fmaf(mk, Jz, acc[5]);
+    }
+    __device__ static void finish(double *, double) {}
+};
+
+// ---------------------------------------------------------------------------
+// The sweep kernel.
+// ---------------------------------------------------------------------------
+struct SplitLaunch {
+    const float4 *irec;
+    const float4 *jrec;
+    uint64_t ni, nj;
+    uint64_t jchunk;      // j-particles per grid j-split
+    double *out[MAX_OUT]; // final outputs (gsplit == 1)
+    double *partial;      // gsplit x NO x ni (gsplit > 1)
+    float eta;
+    double eta_d;
+    unsigned *err;
+};
+
+constexpr int SPLIT_TILE = 256;   // j-records per pipeline stage
+
+__device__ __forceinline__ void kahan_add(float &sum, float &corr, float x)
+{
+    float y = x - corr;
+    float t = sum + y;
+    corr = (t - sum) - y;
+    sum = t;
+}
+
+template <class Op, int NI, int JS, int NT, int MINB>
+__global__ void __launch_bounds__(NT, MINB)
+split_sweep(const SplitLaunch L)
+{
+    constexpr int NF = Op::NF, NO = Op::NO, MAXC = Op::MAXC;
+    constexpr int TJ = SPLIT_TILE;
+    constexpr int FOLD = (64 / JS) > 8 ? (64 / JS) : 8;
+    static_assert(TJ % (JS * FOLD) == 0, "fold must divide the tile");
+    constexpr int GROUPS = NT / JS;          // i-groups per CTA
+    constexpr int IPC = GROUPS * NI;         // i-particles per CTA
+
+    __shared__ __align__(128) float4 ring[2][TJ * NF];
+    __shared__ __align__(8) uint64_t bar[2];
+
+    const int tid = threadIdx.x;
+    const int js = tid % JS;
+    const int grp = tid / JS;
+    const uint64_t ibase = (uint64_t)blockIdx.x * IPC + (uint64_t)grp * NI;
+
+    const uint64_t jb = (uint64_t)blockIdx.y * L.jchunk;
+    const uint64_t je = jb + L.jchunk < L.nj ? jb + L.jchunk : L.nj;
+    const uint64_t jcount = je > jb ? je - jb : 0;
+    const int ntiles = (int)((jcount + TJ - 1) / TJ);
+
+    if (tid == 0) {
+        mbar_init(&bar[0], 1);
+        mbar_init(&bar[1], 1);
+        mbar_init_fence();
+    }
+    __syncthreads();
+
+    auto issue = [&](int t) {
+        const uint64_t j0 = jb + (uint64_t)t * TJ;
+        const uint64_t nrec = (je - j0) < (uint64_t)TJ ? (je - j0) : TJ;
+        const uint32_t bytes = (uint32_t)(nrec * NF * sizeof(float4));
+        mbar_arrive_expect_tx(&bar[t & 1], bytes);
+        bulk_g2s(&ring[t & 1][0], L.jrec + j0 * NF, bytes, &bar[t & 1]);
+    };
+    if (tid == 0) {
+        if (ntiles > 0) issue(0);
+        if (ntiles > 1) issue(1);
+    }
+
+    typename Op::P ip[NI];
+#pragma unroll
+    for (int k = 0; k < NI; ++k) {
+        uint64_t i = ibase + k;
+        if (i >= L.ni) i = L.ni - 1;
+        ip[k] = Op::load(L.irec + i * NF);
+    }
+
+    float sum[NI][NO], corr[NI][NO], part[NI][NO];
+#pragma unroll
+    for (int k = 0; k < NI; ++k)
+#pragma unroll
+        for (int c = 0; c < NO; ++c) sum[k][c] = corr[k][c] = part[k][c] = 0.f;
+
+    auto fold = [&]() {
+#pragma unroll
+        for (int k = 0; k < NI; ++k)
+#pragma unroll
+            for (int c = 0; c < NO; ++c) {
+                if (c == MAXC) sum[k][c] = fmaxf(sum[k][c], part[k][c]);
+                else kahan_add(sum[k][c], corr[k][c], part[k][c]);
+                part[k][c] = 0.f;
+            }
+    };
+
+    bool ok = true;
+    for (int t = 0; t < ntiles; ++t) {
+        bool got = mbar_wait_bounded(&bar[t & 1], (uint32_t)((t >> 1) & 1),
+                                     L.err);
+        if (!__syncthreads_and(got)) { ok = false; break; }
+        const float4 *tile = &ring[t & 1][0];
+        const uint64_t j0 = jb + (uint64_t)t * TJ;
+        const int n = (int)((je - j0) < (uint64_t)TJ ? (je - j0) : TJ);
+        if (n == TJ) {
+#pragma unroll 1
+            for (int r0 = 0; r0 < TJ; r0 += JS * FOLD) {
+#pragma unroll 4
+                for (int u = 0; u < FOLD; ++u) {
+                    const typename Op::P jp =
+                        Op::load(tile + (r0 + u * JS + js) * NF);
+#pragma unroll
+                    for (int k = 0; k < NI; ++k)
+                        Op::pair(ip[k], jp, part[k], L.eta);
+                }
+                fold();
+            }
+        } else {
+#pragma unroll 1
+            for (int r = js; r < n; r += JS) {
+                const typename Op::P jp = Op::load(tile + r * NF);
+#pragma unroll
+                for (int k = 0; k < NI; ++k)
+                    Op::pair(ip[k], jp, part[k], L.eta);
+            }
+            fold();
+        }
+        __syncthreads();
+        if (tid == 0 && t + 2 < ntiles) issue(t + 2);
+    }
+    if (!ok) {
+        // A copy did not complete in time: wait (bounded) for whatever is
+        // still in flight before the shared memory goes away, then leave
+        // without writing results (the host reports the error word).
+        if (tid == 0)
+            for (int s = 0; s < 2; ++s) mbar_wait_bounded(&bar[s], 0, L.err);
+        return;
+    }
+
+    // Combine the lanes that share an i (j-split within the warp).
+#pragma unroll
+    for (int k = 0; k < NI; ++k) {
+        double v[NO];
+#pragma unroll
+        for (int c = 0; c < NO; ++c) {
+            v[c] = (c == MAXC) ? (double)sum[k][c]
+                               : (double)sum[k][c] - (double)corr[k][c];
+#pragma unroll
+            for (int off = JS / 2; off > 0; off >>= 1) {
+                double w = __shfl_xor_sync(0xffffffffu, v[c], off);
+                v[c] = (c == MAXC) ? fmax(v[c], w) : v[c] + w;
+            }
+        }
+        const uint64_t i = ibase + k;
+        if (js == 0 && i < L.ni) {
+            if (gridDim.y == 1) {
+                Op::finish(v, L.eta_d);
+#pragma unroll
+                for (int c = 0; c < NO; ++c) L.out[c][i] = v[c];
+            } else {
+#pragma unroll
+                for (int c = 0; c < NO; ++c)
+                    L.partial[((uint64_t)blockIdx.y * NO + c) * L.ni + i] = v[c];
+            }
+        }
+    }
+}
+
+// Reduce grid j-split partials in a fixed order and apply the finish step.
+template <class Op>
+__global__ void split_finalize(const SplitLaunch L, int gsplit)
+{
+    constexpr int NO = Op::NO, MAXC = Op::MAXC;
+    for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+         i < L.ni; i += (uint64_t)gridDim.x * blockDim.x) {
+        double v[NO];
+#pragma unroll
+        for (int c = 0; c < NO; ++c) {
+            double a = L.partial[(uint64_t)c * L.ni + i];
+            for (int y = 1; y < gsplit; ++y) {
+                double b = L.partial[((uint64_t)y * NO + c) * L.ni + i];
+                a = (c == MAXC) ? fmax(a, b) : a + b;
+            }
+            v[c] = a;
+        }
+        Op::finish(v, L.eta_d);
+#pragma unroll
+        for (int c = 0; c < NO; ++c) L.out[c][i] = v[c];
+    }
+}
+
+// ---------------------------------------------------------------------------
+// Variant table and launcher.
+// ---------------------------------------------------------------------------
+struct VariantInfo {
+    int ni_per_thread, jsplit, threads;
+};
+
+// Variants compiled for every operator; the C-ABI layer picks one.
+static const VariantInfo kVariants[] = {
+    {2, 1, 256},   // large sweeps: two i per thread, whole warp on one j
+    {1, 1, 256},
+    {1, 4, 256},   // fewer i: lanes share an i and split the j-tile
+    {1, 16, 256},
+    {1, 32, 128},
+};
+constexpr int N_VARIANTS = sizeof(kVariants) / sizeof(kVariants[0]);
+
+int split_variant_count() { return N_VARIANTS; }
+
+void split_variant_info(int v, int *ni_per_thread, int *jsplit, int *threads)
+{
+    *ni_per_thread = kVariants[v].ni_per_thread;
+    *jsplit = kVariants[v].jsplit;
+    *threads = kVariants[v].threads;
+}
+
+bool split_supported(int kernel)
+{
+    return kernel == K_PHI || kernel == K_ACC || kernel == K_ACC_JERK ||
+           kernel == K_TSTEP || kernel == K_SNAP_CRACKLE;
+}
+
+template <class Op, int NI, int JS, int NT, int MINB>
+static cudaError_t run_variant(const SplitLaunch &L, int gsplit,
+                               cudaStream_t st)
+{
+    constexpr uint64_t IPC = (uint64_t)(NT / JS) * NI;
+    const uint64_t gx = (L.ni + IPC - 1) / IPC;
+    dim3 grid((unsigned)gx, (unsigned)gsplit);
+    split_sweep<Op, NI, JS, NT, MINB><<<grid, NT, 0, st>>>(L);
+    g_launch_count += 1;
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess || gsplit == 1) return e;
+    uint64_t blocks = (L.ni + 255) / 256;
+    if (blocks > 152 * 8) blocks = 152 * 8;
+    split_finalize<Op><<<(unsigned)blocks, 256, 0, st>>>(L, gsplit);
+    g_launch_count += 1;
+    return cudaGetLastError();
+}
+
+template <class Op>
+static cudaError_t run_op(const SplitLaunch &L, int variant, int gsplit,
+                          cudaStream_t st)
+{
+    switch (variant) {
+    case 0: return run_variant<Op, 2, 1, 256, 2>(L, gsplit, st);
+    case 1: return run_variant<Op, 1, 1, 256, 2>(L, gsplit, st);
+    case 2: return run_variant<Op, 1, 4, 256, 2>(L, gsplit, st);
+    case 3: return run_variant<Op, 1, 16, 256, 2>(L, gsplit, st);
+    case 4: return run_variant<Op, 1, 32, 128, 4>(L, gsplit, st);
+    default: return cudaErrorInvalidValue;
+    }
+}
+
+// irec/jrec: packed records (launch_pack); out: NO double arrays;
+// partial: gsplit x NO x ni doubles when gsplit > 1.
+cudaError_t launch_split(int kernel, const float4 *irec, const float4 *jrec,
+                         uint64_t ni, uint64_t nj, void *const *out,
+                         double *partial, int variant, int gsplit, double eta,
+                         unsigned *err, cudaStream_t st)
+{
+    if (ni == 0) return cudaSuccess;
+    if (gsplit < 1) gsplit = 1;
+    SplitLaunch L;
+    L.irec = irec;
+    L.jrec = jrec;
+    L.ni = ni;
+    L.nj = nj;
+    uint64_t chunk = (nj + gsplit - 1) / gsplit;
+    chunk = (chunk + SPLIT_TILE - 1) / SPLIT_TILE * SPLIT_TILE;
+    if (chunk == 0) chunk = SPLIT_TILE;
+    L.jchunk = chunk;
+    for (int c = 0; c < MAX_OUT; ++c)
+        L.out[c] = c < n_out(kernel) ? (double *)out[c] : nullptr;
+    L.partial = partial;
+    L.eta = (float)eta;
+    L.eta_d = eta;
+    L.err = err;
+    switch (kernel) {
+    case K_PHI: return run_op<PhiS>(L, variant, gsplit, st);
+    case K_ACC: return run_op<AccS>(L, variant, gsplit, st);
+    case K_ACC_JERK: return run_op<AccJerkS>(L, variant, gsplit, st);
+    case K_TSTEP: return run_op<TstepS>(L, variant, gsplit, st);
+    case K_SNAP_CRACKLE: return run_op<SnapS>(L, variant, gsplit, st);
+    default: return cudaErrorInvalidValue;
+    }
+}
+
+}  // namespace tg
