@@ -188,7 +188,8 @@ void tupan_gb300_split_variant_info(int variant, int *ni_per_thread,
  * (j_attrs unused for Kepler); outs: device pointers of its outputs.
  * scal[0] = eta (tstep) or dt (nreg, sakura, kepler); scal[1..7] = 1/c^k
  * (pnacc).  iscal = flag (sakura) or PN order (pnacc).  mode < 0 uses the
- * library mode.  stream may be NULL.  Asynchronous unless sync != 0.
+ * library mode.  stream: a cudaStream_t, NULL meaning the default stream.
+ * Asynchronous unless sync != 0.
  * Returns a status code. */
 int tupan_gb300_dev_sweep(int kernel, int mode, uint64_t ni,
                           const void *const *i_attrs, uint64_t nj,

@@ -1,0 +1,199 @@
+"""Numpy restatement of tupan's Hermite and Sakura integrators -- TEST
+INFRASTRUCTURE ONLY (parity checker for the device-resident drivers).
+
+Each function follows the reference statement by statement, with numpy fp64
+elementwise arithmetic in the same order, and calls the oracle kernels for
+the pairwise sums, so a run is bit-identical to the reference integrator on
+the reference's C backend:
+
+* ``block_tstep``   tupan/integrator/__init__.py:59-78 (get_min_block_tstep)
+* ``base_tstep``    tupan/integrator/__init__.py:48-57 (get_base_tstep)
+* ``hermite_step``  tupan/integrator/hermite.py:20-283 (H2/H4/H6/H8 epredict,
+                    ecorrect, epec) and :390-410 (Hermite.do_step)
+* ``sakura_step``   tupan/integrator/sakura.py:22-50, :100-117 (asakura step)
+* ``evolve``        tupan/simulation.py:187-198 loop over evolve_step
+                    (tupan/integrator/__init__.py:80-99)
+
+A state is a dict of float64 arrays m, rx, ry, rz, e2, vx, vy, vz.
+"""
+
+import math
+import sys
+
+import numpy as np
+
+import oracle
+
+POS = ("rx", "ry", "rz")
+VEL = ("vx", "vy", "vz")
+
+
+def _kern(name, ips, jps=None, scal=None):
+    return oracle.run(name, ips, jps if jps is not None else ips, scal)
+
+
+def base_tstep(t_curr, t_end, eta):
+    """tupan/integrator/__init__.py:48-57"""
+    dt = min(abs(t_end) - abs(t_curr), abs(eta))
+    dt = max(dt, abs(t_end) * (2 * sys.float_info.epsilon))
+    return math.copysign(dt, eta)
+
+
+def block_tstep(min_ts, t_curr, tau):
+    """tupan/integrator/__init__.py:59-78 for a given min |tstep|."""
+    power = int(np.log2(min_ts) - 1)
+    min_bts = 2.0 ** power
+    t_next = t_curr + min_bts
+    while t_next % min_bts != 0:
+        min_bts /= 2
+    min_bts = math.copysign(min_bts, tau)
+    if abs(min_bts) > abs(tau):
+        min_bts = tau
+    return min_bts
+
+
+def forces(order, ps):
+    """set_acc / set_acc_jerk / set_snap_crackle as each Hn.epredict and
+    ecorrect call them (hermite.py:30, :80-81, :132-133, :206-207)."""
+    f = {}
+    if order == 2:
+        f["ax"], f["ay"], f["az"] = _kern("acc_kernel", ps)
+        return f
+    out = _kern("acc_jerk_kernel", ps)
+    for k, v in zip(("ax", "ay", "az", "jx", "jy", "jz"), out):
+        f[k] = v
+    if order >= 6:
+        q = dict(ps)
+        q.update(f)
+        out = _kern("snap_crackle_kernel", q)
+        for k, v in zip(("sx", "sy", "sz", "cx", "cy", "cz"), out):
+            f[k] = v
+    return f
+
+
+def predict(order, ps, f0, tau):
+    """Hn.epredict position/velocity updates (hermite.py:33-38, :83-88,
+    :136-157, :210-235); ps is updated in place from the copy's values."""
+    for c, (r, v) in enumerate(zip(POS, VEL)):
+        a = f0["a" + "xyz"[c]]
+        if order == 2:
+            ps[r] = ps[r] + (a * tau / 2 + ps[v]) * tau
+            ps[v] = ps[v] + a * tau
+            continue
+        j = f0["j" + "xyz"[c]]
+        if order == 4:
+            ps[r] = ps[r] + ((j * tau / 3 + a) * tau / 2 + ps[v]) * tau
+            ps[v] = ps[v] + (j * tau / 2 + a) * tau
+            continue
+        s = f0["s" + "xyz"[c]]
+        if order == 6:
+            ps[r] = ps[r] + (((s * tau / 4 + j) * tau / 3 + a) * tau / 2
+                             + ps[v]) * tau
+            ps[v] = ps[v] + ((s * tau / 3 + j) * tau / 2 + a) * tau
+            continue
+        cr = f0["c" + "xyz"[c]]
+        ps[r] = ps[r] + ((((cr * tau / 5 + s) * tau / 4 + j) * tau / 3 + a)
+                         * tau / 2 + ps[v]) * tau
+        ps[v] = ps[v] + (((cr * tau / 4 + s) * tau / 3 + j) * tau / 2
+                         + a) * tau
+
+
+def correct(order, ps1, ps0, f0, f1, tau):
+    """Hn.ecorrect (hermite.py:46-57, :96-119, :162-195, :238-283).
+    Velocities first, then positions from the corrected velocities."""
+    for c, (r, v) in enumerate(zip(POS, VEL)):
+        x = "xyz"[c]
+        a0, a1 = f0["a" + x], f1["a" + x]
+        if order == 2:
+            ps1[v] = ((a0 + a1) * tau / 2 + ps0[v])
+            ps1[r] = ((ps0[v] + ps1[v]) * tau / 2 + ps0[r])
+            continue
+        j0, j1 = f0["j" + x], f1["j" + x]
+        if order == 4:
+            ps1[v] = (((j0 - j1) * tau / 6 + (a0 + a1)) * tau / 2 + ps0[v])
+            ps1[r] = (((a0 - a1) * tau / 6 + (ps0[v] + ps1[v])) * tau / 2
+                      + ps0[r])
+            continue
+        s0, s1 = f0["s" + x], f1["s" + x]
+        if order == 6:
+            ps1[v] = ((((s0 + s1) * tau / 12 + (j0 - j1)) * tau / 5
+                       + (a0 + a1)) * tau / 2 + ps0[v])
+            ps1[r] = ((((j0 + j1) * tau / 12 + (a0 - a1)) * tau / 5
+                       + (ps0[v] + ps1[v])) * tau / 2 + ps0[r])
+            continue
+        c0, c1 = f0["c" + x], f1["c" + x]
+        ps1[v] = (((((c0 - c1) * tau / 20 + (s0 + s1)) * tau / 3
+                    + 3 * (j0 - j1)) * tau / 14 + (a0 + a1)) * tau / 2
+                  + ps0[v])
+        ps1[r] = (((((s0 - s1) * tau / 20 + (j0 + j1)) * tau / 3
+                    + 3 * (a0 - a1)) * tau / 14 + (ps0[v] + ps1[v])) * tau / 2
+                  + ps0[r])
+
+
+def hermite_step(ps, t_curr, tau, eta, order, adaptive):
+    """Hermite.do_step (hermite.py:390-410) with epec(2, ...) (:60-67).
+    Returns the step taken; ps is advanced in place."""
+    if adaptive:
+        dt_a, dt_b = _kern("tstep_kernel", ps, None, {"eta": eta})
+        tau = block_tstep(np.abs(dt_a).min(), t_curr, tau)
+    ps0 = {k: v.copy() for k, v in ps.items()}
+    f0 = forces(order, ps0)
+    predict(order, ps, f0, tau)
+    for _ in range(2):
+        f1 = forces(order, ps)
+        correct(order, ps, ps0, f0, f1, tau)
+    return tau
+
+
+def sakura_step(ps, tau):
+    """sakura.py:22-50"""
+    for r, v in zip(POS, VEL):
+        ps[r] = ps[r] + ps[v] * tau / 2
+    for flag in (-1, 1):
+        d = _kern("sakura_kernel", ps, None, {"dt": tau / 2, "flag": flag})
+        for k, dv in zip(POS + VEL, d):
+            ps[k] = ps[k] + dv
+    for r, v in zip(POS, VEL):
+        ps[r] = ps[r] + ps[v] * tau / 2
+
+
+def sakura_tstep(ps, eta, t_curr, tau):
+    """Sakura.get_sakura_tstep (sakura.py:100-117)."""
+    dt_a, dt_b = _kern("tstep_kernel", ps, None, {"eta": eta})
+    iw2_a = (eta / dt_a) ** 2
+    iw2_b = (eta / dt_b) ** 2
+    diw2 = (iw2_a - iw2_b)
+    w2_sakura = diw2.max()
+    dt_sakura = eta / (1 + w2_sakura) ** 0.5
+    return block_tstep(abs(dt_sakura), t_curr, tau)
+
+
+def energies(ps):
+    """Kinetic, potential (0.5 sum m phi) energies as body.py:260-321."""
+    ke = 0.5 * ps["m"] * (ps["vx"] ** 2 + ps["vy"] ** 2 + ps["vz"] ** 2)
+    phi = _kern("phi_kernel", ps)[0]
+    pe = ps["m"] * phi
+    return float(ke.sum()), 0.5 * float(pe.sum())
+
+
+def evolve(ps, t_end, eta, method, max_steps=None):
+    """Simulation.evolve (simulation.py:191-198) for one method.  Returns the
+    list of steps taken; ps is advanced in place."""
+    order = {"hermite2": 2, "hermite4": 4, "hermite6": 6, "hermite8": 8}
+    t = 0.0
+    steps = []
+    while abs(t) < t_end:
+        tau = base_tstep(t, t_end, eta)
+        if "sakura" in method:
+            if method == "asakura":
+                tau = sakura_tstep(ps, eta, t, tau)
+            sakura_step(ps, tau)
+        else:
+            meth = method[1:] if method.startswith("a") else method
+            tau = hermite_step(ps, t, tau, eta, order[meth],
+                               method.startswith("a"))
+        t += tau
+        steps.append(tau)
+        if max_steps is not None and len(steps) >= max_steps:
+            break
+    return steps

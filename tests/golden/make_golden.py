@@ -220,5 +220,61 @@ def main(refroot):
             print("wrote", fn, os.path.getsize(fn))
 
 
+INTEGRATOR_RUNS = [
+    # (method, n, eps, masses, eta, t_end, max_steps, seed)
+    ("ahermite4", 64, 1e-4, "equal", 1.0 / 64, 1.0, 60, 11),
+    ("hermite4", 64, 1e-4, "equal", 1.0 / 64, 1.0, 40, 12),
+    ("ahermite6", 48, 1e-4, "salpeter", 1.0 / 32, 0.5, 30, 13),
+    ("ahermite8", 48, 1e-4, "salpeter", 1.0 / 32, 0.5, 30, 14),
+    ("ahermite2", 48, 1e-4, "equal", 1.0 / 64, 1.0, 30, 15),
+    ("sakura", 40, 0.0, "salpeter", 1.0 / 256, 0.25, 20, 16),
+    ("asakura", 40, 0.0, "salpeter", 1.0 / 64, 0.25, 20, 17),
+]
+
+
+def integrators(refroot):
+    """Short runs of the reference's own integrators on its C backend
+    (tupan/integrator/__init__.py:108-157, evolve loop as
+    tupan/simulation.py:191-198)."""
+    sys.path.insert(0, refroot)
+    sys.path.insert(0, os.path.dirname(os.path.dirname(HERE)))
+    from tupan.integrator import Integrator
+    from tupan.particles.allparticles import ParticleSystem
+    from tupan_gb300 import ics
+
+    store = {}
+    for (method, n, eps, masses, eta, t_end, max_steps, seed) in \
+            INTEGRATOR_RUNS:
+        d = ics.plummer(n, eps=eps, seed=seed, masses=masses)
+        ps = ParticleSystem(n)
+        ps.mass[...] = d["m"]
+        ps.eps2[...] = d["e2"]
+        for k in ("rx", "ry", "rz", "vx", "vy", "vz"):
+            getattr(ps, k)[...] = d[k]
+        tag = "%s/" % method
+        for k in ("m", "e2", "rx", "ry", "rz", "vx", "vy", "vz"):
+            store[tag + "in/" + k] = d[k].copy()
+        integ = Integrator(eta, 0.0, ps, method=method)
+        steps = []
+        while abs(integ.time) < t_end and len(steps) < max_steps:
+            t0 = integ.time
+            integ.evolve_step(t_end)
+            steps.append(integ.time - t0)
+        ps = integ.particle_system
+        store[tag + "steps"] = np.array(steps)
+        store[tag + "params"] = np.array([eta, t_end, max_steps])
+        for k in ("rx", "ry", "rz", "vx", "vy", "vz"):
+            store[tag + "out/" + k] = np.array(getattr(ps, k), copy=True)
+        print(method, len(steps), "steps, t =", integ.time)
+    fn = os.path.join(HERE, "golden_integrators.npz")
+    np.savez_compressed(fn, **store)
+    print("wrote", fn, os.path.getsize(fn))
+
+
 if __name__ == "__main__":
-    main(sys.argv[1] if len(sys.argv) > 1 else "/root/reference")
+    ref = sys.argv[1] if len(sys.argv) > 1 else "/root/reference"
+    if "--integrators" in sys.argv:
+        integrators(ref)
+    else:
+        main(ref)
+        integrators(ref)

@@ -1,0 +1,67 @@
+"""Device-resident Hermite driver against tupan's own integrator runs
+(golden_integrators.npz) and the numpy integrator oracle."""
+
+import os
+
+import numpy as np
+import pytest
+
+from oracle import integrators as oi
+from tupan_gb300 import ics
+from tupan_gb300.integrator import DeviceHermite
+
+pytestmark = pytest.mark.gpu
+
+GOLDEN = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden",
+                      "golden_integrators.npz")
+ORDER = {"ahermite2": 2, "ahermite4": 4, "hermite4": 4, "ahermite6": 6,
+         "ahermite8": 8}
+
+
+def load(method):
+    z = np.load(GOLDEN)
+    tag = method + "/"
+    ps = {k: z[tag + "in/" + k].copy() for k in
+          ("m", "e2", "rx", "ry", "rz", "vx", "vy", "vz")}
+    eta, t_end, max_steps = z[tag + "params"]
+    out = {k: z[tag + "out/" + k] for k in
+           ("rx", "ry", "rz", "vx", "vy", "vz")}
+    return ps, float(eta), float(t_end), int(max_steps), z[tag + "steps"], out
+
+
+@pytest.mark.parametrize("method", list(ORDER))
+@pytest.mark.parametrize("batch", [1, 7])
+def test_exact_hermite_bit_identical_to_reference(method, batch):
+    ps, eta, t_end, max_steps, steps, out = load(method)
+    h = DeviceHermite(ps, eta, order=ORDER[method],
+                      adaptive=method.startswith("a"), mode="exact",
+                      record_steps=1000)
+    h.evolve(t_end, max_steps=max_steps, batch=batch)
+    np.testing.assert_array_equal(h.steps(), steps)
+    got = h.state()
+    for k, v in out.items():
+        np.testing.assert_array_equal(got[k], v)
+    h.close()
+
+
+def test_split_hermite4_energy_and_steps():
+    # Config 1 shape (Plummer, eta = 1/64, eps = 1e-4) over a short time:
+    # SPLIT forces keep the energy error of the fp64 run.
+    ps = ics.plummer(256, eps=1e-4, seed=1)
+    ref = {k: v.copy() for k, v in ps.items()}
+    ke0, pe0 = oi.energies(ref)
+    steps = oi.evolve(ref, 0.0625, 1.0 / 64, "ahermite4")
+    ke1, pe1 = oi.energies(ref)
+    de_ref = ((ke1 + pe1) - (ke0 + pe0)) / -pe0
+    h = DeviceHermite(ps, 1.0 / 64, order=4, adaptive=True, mode="split",
+                      record_steps=100000)
+    k0, p0 = h.energy()
+    assert abs(k0 - ke0) <= 1e-12 * abs(ke0)
+    assert abs(p0 - pe0) <= 1e-6 * abs(pe0)
+    h.evolve(0.0625, batch=16)
+    k1, p1 = h.energy()
+    de = ((k1 + p1) - (k0 + p0)) / -p0
+    assert abs(h.time - 0.0625) == 0.0
+    assert abs(de) <= max(10 * abs(de_ref), 1e-10), (de, de_ref)
+    assert len(h.steps()) == len(steps)
+    h.close()

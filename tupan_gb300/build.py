@@ -31,9 +31,10 @@ UNITS = {
     "abi64.o": ("abi.cu", ["-DTG_ABI_FLOAT64"]),
     "abi32.o": ("abi.cu", ["-DTG_ABI_FLOAT32"]),
     "microbench.o": ("microbench.cu", []),
+    "driver.o": ("driver.cu", ["-fmad=false"]),
 }
 LINKS = {
-    LIB64: ["exact.o", "split.o", "abi64.o", "microbench.o"],
+    LIB64: ["exact.o", "split.o", "abi64.o", "microbench.o", "driver.o"],
     LIB32: ["exact.o", "split.o", "abi32.o", "microbench.o"],
 }
 

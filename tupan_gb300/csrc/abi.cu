@@ -411,6 +411,21 @@ void fill_side(const REAL **dst, std::initializer_list<const REAL *> src)
 }  // namespace
 
 namespace tg {
+// Split configuration for callers inside the library (the drivers).
+void choose_split_public(int kernel, uint64_t ni, uint64_t nj, int *variant,
+                         int *gsplit)
+{
+    std::lock_guard<std::mutex> lock(g_mu);
+    init_overrides();
+    DeviceState *d;
+    if (device_state(&d)) {
+        *variant = 0;
+        *gsplit = 1;
+        return;
+    }
+    choose_split(d, kernel, ni, nj, variant, gsplit);
+}
+
 int split_nf_host(int k)
 {
     return (k == K_PHI || k == K_ACC) ? 2 : (k == K_SNAP_CRACKLE ? 5 : 3);
@@ -732,8 +747,8 @@ TG_EXPORT void tupan_gb300_split_variant_info(int v, int *ni_per_thread,
     split_variant_info(v, ni_per_thread, jsplit, threads);
 }
 
-// One sweep over DEVICE arrays on a caller's stream (nullptr: the library's
-// stream).  i_attrs/j_attrs: host arrays of n_attr(kernel) device pointers
+// One sweep over DEVICE arrays on a caller's stream (NULL: the legacy
+// default stream).  i_attrs/j_attrs: host arrays of n_attr(kernel) device pointers
 // in libtupan.h order; outs: n_out(kernel) device pointers; scal: eta or dt
 // in scal[0], 1/c^k in scal[k] for PNAcc; iscal: flag or PN order.  Returns
 // 0 or a status code.  Asynchronous unless `sync` is non-zero, in which case
@@ -755,7 +770,7 @@ TG_EXPORT int tupan_gb300_dev_sweep(int kernel, int mode, uint64_t ni,
     DeviceState *d;
     int rc = device_state(&d);
     if (rc) return rc;
-    cudaStream_t st = stream ? (cudaStream_t)stream : d->stream;
+    cudaStream_t st = (cudaStream_t)stream;   // NULL: the default stream
     Sweep s;
     memset(&s, 0, sizeof(s));
     s.kernel = kernel;

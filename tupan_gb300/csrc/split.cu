@@ -297,7 +297,9 @@ split_sweep(const SplitLaunch L)
 {
     constexpr int NF = Op::NF, NO = Op::NO, MAXC = Op::MAXC;
     constexpr int TJ = SPLIT_TILE;
-    constexpr int FOLD = (64 / JS) > 8 ? (64 / JS) : 8;
+    // Records per lane summed in FP32 before a Kahan fold: short runs keep
+    // the FP32 rounding of each run small next to the particle's |a|.
+    constexpr int FOLD = (TJ / JS) < 16 ? (TJ / JS) : 16;
     static_assert(TJ % (JS * FOLD) == 0, "fold must divide the tile");
     constexpr int GROUPS = NT / JS;          // i-groups per CTA
     constexpr int IPC = GROUPS * NI;         // i-particles per CTA
@@ -370,7 +372,7 @@ split_sweep(const SplitLaunch L)
         if (n == TJ) {
 #pragma unroll 1
             for (int r0 = 0; r0 < TJ; r0 += JS * FOLD) {
-#pragma unroll 4
+#pragma unroll
                 for (int u = 0; u < FOLD; ++u) {
                     const typename Op::P jp =
                         Op::load(tile + (r0 + u * JS + js) * NF);

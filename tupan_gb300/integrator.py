@@ -1,0 +1,114 @@
+"""Device-resident integrators on the CUDA library.
+
+``DeviceHermite`` keeps one particle system in HBM and advances it with
+tupan's Hermite scheme (tupan/integrator/hermite.py: H2/H4/H6/H8, P(EC)^2,
+shared steps; ``adaptive=True`` is tupan's "ahermiteN" with the Tstep kernel
+and power-of-two quantisation of tupan/integrator/__init__.py:59-78).  Steps
+are replayed from a CUDA graph; the host only reads the time between
+batches.  With ``mode="exact"`` a run is bit-identical to tupan's own
+integrator on its C backend.
+"""
+
+import ctypes
+
+import numpy as np
+
+from . import lib
+
+_DP = ctypes.POINTER(ctypes.c_double)
+
+
+def _declare(L):
+    c = ctypes
+    L.tupan_gb300_hermite_create.argtypes = (
+        [c.c_uint64, c.c_int, c.c_int, c.c_int, c.c_double] + [_DP] * 8
+        + [c.c_longlong, c.POINTER(c.c_void_p)])
+    L.tupan_gb300_hermite_create.restype = c.c_int
+    L.tupan_gb300_hermite_evolve.argtypes = [
+        c.c_void_p, c.c_double, c.c_longlong, c.c_int, _DP,
+        c.POINTER(c.c_longlong)]
+    L.tupan_gb300_hermite_evolve.restype = c.c_int
+    L.tupan_gb300_hermite_get_state.argtypes = [c.c_void_p] + [_DP] * 6
+    L.tupan_gb300_hermite_get_state.restype = c.c_int
+    L.tupan_gb300_hermite_tau_log.argtypes = [c.c_void_p, _DP, c.c_longlong]
+    L.tupan_gb300_hermite_tau_log.restype = c.c_longlong
+    L.tupan_gb300_hermite_energy.argtypes = [c.c_void_p, _DP, _DP]
+    L.tupan_gb300_hermite_energy.restype = c.c_int
+    L.tupan_gb300_hermite_destroy.argtypes = [c.c_void_p]
+    L.tupan_gb300_hermite_destroy.restype = c.c_int
+
+
+def _p(a):
+    return a.ctypes.data_as(_DP)
+
+
+class DeviceHermite(object):
+    """One N-body system integrated on the GPU."""
+
+    def __init__(self, ps, eta, order=4, adaptive=True, mode="split",
+                 record_steps=0):
+        self.L = lib.load("float64")
+        _declare(self.L)
+        self.n = len(ps["m"])
+        self.eta = float(eta)
+        arrs = [np.ascontiguousarray(ps[k], dtype=np.float64)
+                for k in ("m", "e2", "rx", "ry", "rz", "vx", "vy", "vz")]
+        h = ctypes.c_void_p()
+        st = self.L.tupan_gb300_hermite_create(
+            self.n, int(order), 1 if adaptive else 0,
+            lib.MODE_SPLIT if mode == "split" else lib.MODE_EXACT,
+            self.eta, *[_p(a) for a in arrs], int(record_steps),
+            ctypes.byref(h))
+        if st:
+            raise lib.TupanGB300Error("hermite_create failed: status %d" % st)
+        self.h = h
+        self.time = 0.0
+        self.nsteps = 0
+
+    def evolve(self, t_end, max_steps=0, batch=16):
+        t = ctypes.c_double()
+        k = ctypes.c_longlong()
+        st = self.L.tupan_gb300_hermite_evolve(self.h, float(t_end),
+                                               int(max_steps), int(batch),
+                                               ctypes.byref(t),
+                                               ctypes.byref(k))
+        if st:
+            raise lib.TupanGB300Error("hermite_evolve failed: status %d" % st)
+        self.time = t.value
+        self.nsteps = k.value
+        return self.time
+
+    def state(self):
+        out = {k: np.empty(self.n) for k in ("rx", "ry", "rz", "vx", "vy",
+                                             "vz")}
+        st = self.L.tupan_gb300_hermite_get_state(
+            self.h, *[_p(out[k]) for k in ("rx", "ry", "rz", "vx", "vy",
+                                           "vz")])
+        if st:
+            raise lib.TupanGB300Error("hermite_get_state failed")
+        return out
+
+    def steps(self, cap=1 << 20):
+        buf = np.empty(cap)
+        k = self.L.tupan_gb300_hermite_tau_log(self.h, _p(buf), cap)
+        return buf[:k].copy()
+
+    def energy(self):
+        ke = ctypes.c_double()
+        pe = ctypes.c_double()
+        st = self.L.tupan_gb300_hermite_energy(self.h, ctypes.byref(ke),
+                                               ctypes.byref(pe))
+        if st:
+            raise lib.TupanGB300Error("hermite_energy failed")
+        return ke.value, pe.value
+
+    def close(self):
+        if self.h:
+            self.L.tupan_gb300_hermite_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
