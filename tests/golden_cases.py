@@ -21,7 +21,7 @@ PN = dict(order=7, **{"inv%d" % k: (1.0 / C) ** k for k in range(1, 8)})
 
 
 def files():
-    return sorted(glob.glob(os.path.join(HERE, "golden_*.npz")))
+    return sorted(glob.glob(os.path.join(HERE, "golden_*_float*.npz")))
 
 
 def load(path):
