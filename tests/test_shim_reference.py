@@ -1,0 +1,74 @@
+"""The shim installs the CUDA backend into the reference's own extension
+module (host logic only; runs where the reference tree is importable).
+
+The reference is imported in a child process whose HOME and TMPDIR point
+into the repository's build folder: importing tupan builds its cffi
+libraries under ~/.tupan and opens a log file in the temp directory."""
+
+import json
+import os
+import subprocess
+import sys
+
+import pytest
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+REF = os.environ.get("TUPAN_REFERENCE", "/root/reference")
+
+CHILD = r"""
+import json, sys
+sys.path.insert(0, sys.argv[1]); sys.path.insert(0, sys.argv[2])
+import numpy as np
+from tupan.lib import extensions as ext
+from tupan_gb300 import shim
+from tupan_gb300.backend import CUDAKernel
+shim.install(extensions=ext)
+res = {"singletons": {a: isinstance(getattr(ext, a).kernel, CUDAKernel)
+                      for a, _ in shim.SINGLETONS},
+       "backend": ext.backend,
+       "c_kernel": type(ext.get_kernel("acc_kernel", "C", "float64")).__name__}
+try:
+    ext.get_kernel("acc_kernel", "OpenGL", "float64")
+    res["bad_backend"] = "accepted"
+except ValueError:
+    res["bad_backend"] = "ValueError"
+from tupan.particles.allparticles import ParticleSystem
+ps = ParticleSystem(5)
+ps.mass[...] = 1.0
+aj = ext.AccJerk("CUDA", "float64")
+aj.set_args(ps, ps)
+res["nargs"] = len(aj.kernel.args)
+res["ni"] = int(aj.kernel.args[0])
+res["registered"] = "jx" in ps.__dict__ and str(ps.jx.dtype) == "float64"
+print(json.dumps(res))
+"""
+
+
+@pytest.fixture(scope="module")
+def child():
+    if not os.path.isdir(os.path.join(REF, "tupan")):
+        pytest.skip("reference tree not present")
+    home = os.path.join(ROOT, "_build", "reference_home")
+    os.makedirs(home, exist_ok=True)
+    env = dict(os.environ, HOME=home, TMPDIR=home)
+    r = subprocess.run([sys.executable, "-c", CHILD, REF, ROOT], env=env,
+                       stdout=subprocess.PIPE, stderr=subprocess.PIPE,
+                       text=True, timeout=600)
+    if r.returncode != 0:
+        pytest.skip("reference not importable here: %s" % r.stderr[-300:])
+    return json.loads(r.stdout.strip().splitlines()[-1])
+
+
+def test_singletons_use_cuda_kernels(child):
+    assert all(child["singletons"].values()), child["singletons"]
+    assert child["backend"] == "CUDA"
+
+
+def test_other_backends_still_resolve(child):
+    assert child["c_kernel"] == "CKernel"
+    assert child["bad_backend"] == "ValueError"
+
+
+def test_set_args_marshals_like_reference(child):
+    assert child["nargs"] == 24 and child["ni"] == 5
+    assert child["registered"]

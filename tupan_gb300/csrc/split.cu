@@ -16,6 +16,8 @@
 // The j - i sign convention is used throughout (the reference forms i - j
 // and subtracts); every output is the same quantity.
 
+#include <type_traits>
+
 #include "tg_common.cuh"
 #include "tg_tma.cuh"
 
@@ -267,6 +269,115 @@ struct SnapS {
 };
 
 // ---------------------------------------------------------------------------
+// Two i-particles per thread in packed FP32 (f32x2: .x first i, .y second).
+// One FFMA2/FADD2/FMUL2 does the same operation for both i against the same
+// j, halving the instructions issued per interaction so that the FMA pipe,
+// not instruction issue, bounds the sweep.  i-side positions and velocities
+// are kept negated so that every difference is an addition.
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ float2 dup(float a) { return make_float2(a, a); }
+__device__ __forceinline__ float2 add2(float2 a, float2 b) { return __fadd2_rn(a, b); }
+__device__ __forceinline__ float2 mul2(float2 a, float2 b) { return __fmul2_rn(a, b); }
+__device__ __forceinline__ float2 fma2(float2 a, float2 b, float2 c) { return __ffma2_rn(a, b, c); }
+
+struct PosI2 { float2 nxh, nyh, nzh, nxl, nyl, nzl, e2; };
+struct PosVelI2 { float2 nxh, nyh, nzh, nxl, nyl, nzl, e2, nvx, nvy, nvz; };
+
+// rsqrt with one Newton step on both lanes: y (3/2 - s y^2 / 2), masked to 0
+// where s == h2 (r2 == 0: self pairs and coincident particles).
+__device__ __forceinline__ float2 rsqrt_nr2(float2 s, float2 h2)
+{
+    float2 y = make_float2(rsqrtf(s.x), rsqrtf(s.y));
+    float2 u = mul2(mul2(s, y), y);
+    y = mul2(y, fma2(u, dup(-0.5f), dup(1.5f)));
+    y.x = (s.x > h2.x) ? y.x : 0.0f;
+    y.y = (s.y > h2.y) ? y.y : 0.0f;
+    return y;
+}
+
+struct PhiS2 {
+    using P = PhiS::P;
+    using I = PosI2;
+    __device__ static I pack(const P &a, const P &b)
+    {
+        return {make_float2(-a.xh, -b.xh), make_float2(-a.yh, -b.yh),
+                make_float2(-a.zh, -b.zh), make_float2(-a.xl, -b.xl),
+                make_float2(-a.yl, -b.yl), make_float2(-a.zl, -b.zl),
+                make_float2(a.e2, b.e2)};
+    }
+    __device__ static void pair(const I &i, const P &j, float2 *acc, float)
+    {
+        float2 dx = add2(add2(dup(j.xh), i.nxh), add2(dup(j.xl), i.nxl));
+        float2 dy = add2(add2(dup(j.yh), i.nyh), add2(dup(j.yl), i.nyl));
+        float2 dz = add2(add2(dup(j.zh), i.nzh), add2(dup(j.zl), i.nzl));
+        float2 h2 = add2(i.e2, dup(j.e2));
+        float2 s = fma2(dz, dz, fma2(dy, dy, fma2(dx, dx, h2)));
+        float2 y = rsqrt_nr2(s, h2);
+        acc[0] = fma2(dup(-j.m), y, acc[0]);
+    }
+};
+
+struct AccS2 {
+    using P = PhiS::P;
+    using I = PosI2;
+    __device__ static I pack(const P &a, const P &b) { return PhiS2::pack(a, b); }
+    __device__ static void pair(const I &i, const P &j, float2 *acc, float)
+    {
+        float2 dx = add2(add2(dup(j.xh), i.nxh), add2(dup(j.xl), i.nxl));
+        float2 dy = add2(add2(dup(j.yh), i.nyh), add2(dup(j.yl), i.nyl));
+        float2 dz = add2(add2(dup(j.zh), i.nzh), add2(dup(j.zl), i.nzl));
+        float2 h2 = add2(i.e2, dup(j.e2));
+        float2 s = fma2(dz, dz, fma2(dy, dy, fma2(dx, dx, h2)));
+        float2 y = rsqrt_nr2(s, h2);
+        float2 mk = mul2(mul2(dup(j.m), y), mul2(y, y));
+        acc[0] = fma2(mk, dx, acc[0]);
+        acc[1] = fma2(mk, dy, acc[1]);
+        acc[2] = fma2(mk, dz, acc[2]);
+    }
+};
+
+struct AccJerkS2 {
+    using P = AccJerkS::P;
+    using I = PosVelI2;
+    __device__ static I pack(const P &a, const P &b)
+    {
+        return {make_float2(-a.xh, -b.xh), make_float2(-a.yh, -b.yh),
+                make_float2(-a.zh, -b.zh), make_float2(-a.xl, -b.xl),
+                make_float2(-a.yl, -b.yl), make_float2(-a.zl, -b.zl),
+                make_float2(a.e2, b.e2),   make_float2(-a.vx, -b.vx),
+                make_float2(-a.vy, -b.vy), make_float2(-a.vz, -b.vz)};
+    }
+    __device__ static void pair(const I &i, const P &j, float2 *acc, float)
+    {
+        float2 dx = add2(add2(dup(j.xh), i.nxh), add2(dup(j.xl), i.nxl));
+        float2 dy = add2(add2(dup(j.yh), i.nyh), add2(dup(j.yl), i.nyl));
+        float2 dz = add2(add2(dup(j.zh), i.nzh), add2(dup(j.zl), i.nzl));
+        float2 ux = add2(dup(j.vx), i.nvx);
+        float2 uy = add2(dup(j.vy), i.nvy);
+        float2 uz = add2(dup(j.vz), i.nvz);
+        float2 h2 = add2(i.e2, dup(j.e2));
+        float2 s = fma2(dz, dz, fma2(dy, dy, fma2(dx, dx, h2)));
+        float2 rv = fma2(dz, uz, fma2(dy, uy, mul2(dx, ux)));
+        float2 y = rsqrt_nr2(s, h2);
+        float2 y2 = mul2(y, y);
+        float2 mk = mul2(mul2(dup(j.m), y), y2);
+        float2 nal = mul2(mul2(rv, dup(-3.0f)), y2);
+        acc[0] = fma2(mk, dx, acc[0]);
+        acc[1] = fma2(mk, dy, acc[1]);
+        acc[2] = fma2(mk, dz, acc[2]);
+        acc[3] = fma2(mk, fma2(nal, dx, ux), acc[3]);
+        acc[4] = fma2(mk, fma2(nal, dy, uy), acc[4]);
+        acc[5] = fma2(mk, fma2(nal, dz, uz), acc[5]);
+    }
+};
+
+// Packed-pair partner of each scalar operator (void: none).
+template <class Op> struct X2Of { using type = void; };
+template <> struct X2Of<PhiS> { using type = PhiS2; };
+template <> struct X2Of<AccS> { using type = AccS2; };
+template <> struct X2Of<AccJerkS> { using type = AccJerkS2; };
+
+// ---------------------------------------------------------------------------
 // The sweep kernel.
 // ---------------------------------------------------------------------------
 struct SplitLaunch {
@@ -291,10 +402,12 @@ __device__ __forceinline__ void kahan_add(float &sum, float &corr, float x)
     sum = t;
 }
 
-template <class Op, int NI, int JS, int NT, int MINB>
+template <class Op, int NI, int JS, int NT, int MINB, bool X2>
 __global__ void __launch_bounds__(NT, MINB)
 split_sweep(const SplitLaunch L)
 {
+    using OpX2 = typename X2Of<Op>::type;
+    static_assert(!X2 || NI == 2, "packed variant handles two i per thread");
     constexpr int NF = Op::NF, NO = Op::NO, MAXC = Op::MAXC;
     constexpr int TJ = SPLIT_TILE;
     // Records per lane summed in FP32 before a Kahan fold: short runs keep
@@ -369,7 +482,37 @@ split_sweep(const SplitLaunch L)
         const float4 *tile = &ring[t & 1][0];
         const uint64_t j0 = jb + (uint64_t)t * TJ;
         const int n = (int)((je - j0) < (uint64_t)TJ ? (je - j0) : TJ);
-        if (n == TJ) {
+        if constexpr (X2) {
+            // packed path: both i of this thread in one float2 per quantity
+            const typename OpX2::I ip2 = OpX2::pack(ip[0], ip[1]);
+#pragma unroll 1
+            for (int r0 = js; r0 < n; r0 += JS * FOLD) {
+                float2 p2[NO];
+#pragma unroll
+                for (int c = 0; c < NO; ++c) p2[c] = make_float2(0.f, 0.f);
+                if (n == TJ) {
+#pragma unroll
+                    for (int u = 0; u < FOLD; ++u) {
+                        const typename Op::P jp =
+                            Op::load(tile + (r0 + u * JS) * NF);
+                        OpX2::pair(ip2, jp, p2, L.eta);
+                    }
+                } else {
+#pragma unroll 1
+                    for (int u = 0; u < FOLD && r0 + u * JS < n; ++u) {
+                        const typename Op::P jp =
+                            Op::load(tile + (r0 + u * JS) * NF);
+                        OpX2::pair(ip2, jp, p2, L.eta);
+                    }
+                }
+#pragma unroll
+                for (int c = 0; c < NO; ++c) {
+                    part[0][c] = p2[c].x;
+                    part[1 % NI][c] = p2[c].y;
+                }
+                fold();
+            }
+        } else if (n == TJ) {
 #pragma unroll 1
             for (int r0 = 0; r0 < TJ; r0 += JS * FOLD) {
 #pragma unroll
@@ -470,6 +613,8 @@ static const VariantInfo kVariants[] = {
     {1, 4, 256},   // fewer i: lanes share an i and split the j-tile
     {1, 16, 256},
     {1, 32, 128},
+    {2, 1, 256},   // as 0 with packed FP32 pairs (phi, acc, acc_jerk)
+    {2, 4, 256},   // packed, lanes split the j-tile
 };
 constexpr int N_VARIANTS = sizeof(kVariants) / sizeof(kVariants[0]);
 
@@ -488,14 +633,14 @@ bool split_supported(int kernel)
            kernel == K_TSTEP || kernel == K_SNAP_CRACKLE;
 }
 
-template <class Op, int NI, int JS, int NT, int MINB>
+template <class Op, int NI, int JS, int NT, int MINB, bool X2 = false>
 static cudaError_t run_variant(const SplitLaunch &L, int gsplit,
                                cudaStream_t st)
 {
     constexpr uint64_t IPC = (uint64_t)(NT / JS) * NI;
     const uint64_t gx = (L.ni + IPC - 1) / IPC;
     dim3 grid((unsigned)gx, (unsigned)gsplit);
-    split_sweep<Op, NI, JS, NT, MINB><<<grid, NT, 0, st>>>(L);
+    split_sweep<Op, NI, JS, NT, MINB, X2><<<grid, NT, 0, st>>>(L);
     g_launch_count += 1;
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess || gsplit == 1) return e;
@@ -516,6 +661,15 @@ static cudaError_t run_op(const SplitLaunch &L, int variant, int gsplit,
     case 2: return run_variant<Op, 1, 4, 256, 2>(L, gsplit, st);
     case 3: return run_variant<Op, 1, 16, 256, 2>(L, gsplit, st);
     case 4: return run_variant<Op, 1, 32, 128, 4>(L, gsplit, st);
+    case 5:
+    case 6:
+        if constexpr (!std::is_void<typename X2Of<Op>::type>::value) {
+            if (variant == 5) return run_variant<Op, 2, 1, 256, 2, true>(L, gsplit, st);
+            return run_variant<Op, 2, 4, 256, 2, true>(L, gsplit, st);
+        } else {
+            if (variant == 5) return run_variant<Op, 2, 1, 256, 2>(L, gsplit, st);
+            return run_variant<Op, 1, 4, 256, 2>(L, gsplit, st);
+        }
     default: return cudaErrorInvalidValue;
     }
 }
