@@ -45,8 +45,9 @@ def test_exact_hermite_bit_identical_to_reference(method, batch):
 
 
 def test_split_hermite4_energy_and_steps():
-    # Config 1 shape (Plummer, eta = 1/64, eps = 1e-4) over a short time:
-    # SPLIT forces keep the energy error of the fp64 run.
+    # Config 1 shape (Plummer, eta = 1/64, eps = 1e-4) over a short time.
+    # The energy diagnostic is fp64; SPLIT forces add FP32 force noise, so
+    # the bound is the fp64 run's error or 1e-9, whichever is larger.
     ps = ics.plummer(256, eps=1e-4, seed=1)
     ref = {k: v.copy() for k, v in ps.items()}
     ke0, pe0 = oi.energies(ref)
@@ -57,11 +58,11 @@ def test_split_hermite4_energy_and_steps():
                       record_steps=100000)
     k0, p0 = h.energy()
     assert abs(k0 - ke0) <= 1e-12 * abs(ke0)
-    assert abs(p0 - pe0) <= 1e-6 * abs(pe0)
+    assert abs(p0 - pe0) <= 1e-12 * abs(pe0)
     h.evolve(0.0625, batch=16)
     k1, p1 = h.energy()
     de = ((k1 + p1) - (k0 + p0)) / -p0
     assert abs(h.time - 0.0625) == 0.0
-    assert abs(de) <= max(10 * abs(de_ref), 1e-10), (de, de_ref)
+    assert abs(de) <= max(10 * abs(de_ref), 1e-9), (de, de_ref)
     assert len(h.steps()) == len(steps)
     h.close()

@@ -554,15 +554,20 @@ TG_EXPORT long long tupan_gb300_hermite_tau_log(void *handle, double *out,
     return k;
 }
 
-// Total kinetic and potential energy (body.py:260-321), potential from a Phi
-// sweep in the system's mode; sums in fp64 on the device.
+// Total kinetic and potential energy (body.py:260-321).  The diagnostic is
+// FP64 whatever the integration mode: the potential comes from an EXACT Phi
+// sweep and the sums are fp64 on the device.
 TG_EXPORT int tupan_gb300_hermite_energy(void *handle, double *ke, double *pe)
 {
     Hermite *h = (Hermite *)handle;
     if (!h) return ST_BAD_ARGUMENT;
     const double *at[5] = {h->A.m, h->A.r[0], h->A.r[1], h->A.r[2], h->A.e2};
     double *out[1] = {h->phi};
-    if (sweep(h, K_PHI, at, out, 0.0) != cudaSuccess) return ST_CUDA;
+    const int mode = h->mode;
+    h->mode = MODE_EXACT;
+    cudaError_t se = sweep(h, K_PHI, at, out, 0.0);
+    h->mode = mode;
+    if (se != cudaSuccess) return ST_CUDA;
     const int blocks = 1024;
     k_energy<<<blocks, 256, 0, h->stream>>>(h->A.m, h->v3, h->phi, h->n,
                                             h->epart);
