@@ -213,6 +213,37 @@ unsigned long long tupan_gb300_launch_count(void);
 double tupan_gb300_fma_sweep(int iters, void *stream);
 double tupan_gb300_fp32_peak_tflops(int iters, int reps);
 
+
+/* ------------------------------------------------------------------------
+ * Device-resident Hermite driver (libtupan_gb300.so only).  No counterpart
+ * in the reference, whose integrators (tupan/integrator/hermite.py:286-410)
+ * keep particles in host arrays and call the kernels once per force
+ * evaluation.  One system stays in HBM; a step follows Hermite.do_step with
+ * epec(2) and, when adaptive, the Tstep kernel plus the power-of-two rule of
+ * tupan/integrator/__init__.py:59-78, all on the device.
+ * ---------------------------------------------------------------------- */
+/* order 2/4/6/8; adaptive 1 = "ahermiteN"; mode 0 EXACT, 1 SPLIT; host
+ * arrays are copied in; tau_log_cap step sizes are recorded. */
+int tupan_gb300_hermite_create(uint64_t n, int order, int adaptive, int mode,
+                               double eta, const double *m, const double *e2,
+                               const double *rx, const double *ry,
+                               const double *rz, const double *vx,
+                               const double *vy, const double *vz,
+                               long long tau_log_cap, void **handle);
+/* Steps until |t| >= t_end or max_steps (0: no limit) steps were taken,
+ * replaying a CUDA graph of `batch` steps between host checks. */
+int tupan_gb300_hermite_evolve(void *handle, double t_end,
+                               long long max_steps, int batch, double *t_out,
+                               long long *steps_out);
+int tupan_gb300_hermite_get_state(void *handle, double *rx, double *ry,
+                                  double *rz, double *vx, double *vy,
+                                  double *vz);
+long long tupan_gb300_hermite_tau_log(void *handle, double *out,
+                                      long long cap);
+/* Kinetic and potential energy, fp64 (EXACT Phi sweep). */
+int tupan_gb300_hermite_energy(void *handle, double *ke, double *pe);
+int tupan_gb300_hermite_destroy(void *handle);
+
 #ifdef __cplusplus
 }
 #endif

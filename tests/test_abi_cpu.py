@@ -32,10 +32,19 @@ def built():
     return True
 
 
+def float64_only():
+    """Header functions the float32 library does not export (the device
+    drivers work on double data only)."""
+    return {n for n in header_functions()
+            if n.startswith("tupan_gb300_hermite_")}
+
+
 @pytest.mark.parametrize("prec", ["float64", "float32"])
 def test_library_exports_every_header_symbol(built, prec):
     L = ctypes.CDLL(lib.library_path(prec))
-    missing = [n for n in header_functions() if not hasattr(L, n)]
+    skip = float64_only() if prec == "float32" else set()
+    missing = [n for n in header_functions()
+               if n not in skip and not hasattr(L, n)]
     assert not missing, missing
 
 
