@@ -249,13 +249,17 @@ def _block_forces(order, I, J):
 
 
 def block_init(ps, order, eta, dt_max):
+    """Forces and steps of all particles at t = 0: acc/jerk first, then (for
+    orders 6 and 8) snap/crackle with those a, j on both sides."""
     st = {k: v.copy() for k, v in ps.items() if k in
           ("m", "e2", "rx", "ry", "rz", "vx", "vy", "vz")}
-    f = _block_forces(order, st, st)
-    st.update(f)
-    for d in DER[order]:
-        for c in "xyz":
-            st.setdefault(d + c, np.zeros_like(st["m"]))
+    out = oracle.run("acc_jerk_kernel", st, st)
+    for k, v in zip(("ax", "ay", "az", "jx", "jy", "jz"), out):
+        st[k] = v
+    if order >= 6:
+        out = oracle.run("snap_crackle_kernel", st, st)
+        for k, v in zip(("sx", "sy", "sz", "cx", "cy", "cz"), out):
+            st[k] = v
     dt_a = oracle.run("tstep_kernel", st, st, {"eta": eta})[0]
     st["dt"] = np.array([block_tstep(abs(x), 0.0, dt_max) for x in dt_a])
     st["t"] = np.zeros_like(st["m"])

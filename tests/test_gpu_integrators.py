@@ -66,3 +66,47 @@ def test_split_hermite4_energy_and_steps():
     assert abs(de) <= max(10 * abs(de_ref), 1e-9), (de, de_ref)
     assert len(h.steps()) == len(steps)
     h.close()
+
+
+# ---------------------------------------------------------------------------
+# Individual block time steps
+# ---------------------------------------------------------------------------
+from tupan_gb300.integrator import DeviceBlockHermite  # noqa: E402
+
+
+@pytest.mark.parametrize("order", [4, 6, 8])
+def test_exact_block_steps_bit_identical_to_oracle(order):
+    ps = ics.plummer(96, eps=1e-4, seed=40 + order, masses="salpeter")
+    eta, dt_max = 1.0 / 32, 1.0 / 16
+    st = oi.block_init(ps, order, eta, dt_max)
+    active = []
+    for _ in range(40):
+        t, na = oi.block_step(st, order, eta, dt_max)
+        active.append(na)
+    assert min(active) < len(ps["m"])          # the sets really vary
+    b = DeviceBlockHermite(ps, eta, dt_max, order=order, mode="exact")
+    b.evolve(1e30, max_steps=40)
+    assert b.time == t
+    assert b.active == sum(active)
+    got = b.state()
+    for k in ("rx", "ry", "rz", "vx", "vy", "vz", "t", "dt"):
+        np.testing.assert_array_equal(got[k], st[k], err_msg=k)
+    b.close()
+
+
+def test_split_block_steps_energy():
+    ps = ics.plummer(2048, eps=1e-4, seed=3, masses="salpeter")
+    eta, dt_max, t_end = 1.0 / 32, 1.0 / 32, 1.0 / 16
+    k0, p0 = oi.energies(ps)
+    b = DeviceBlockHermite(ps, eta, dt_max, order=6, mode="split")
+    b.evolve(t_end)
+    assert b.time == t_end
+    got = b.state()
+    assert np.all(got["t"] == t_end)
+    fin = dict(ps)
+    fin.update({k: got[k] for k in ("rx", "ry", "rz", "vx", "vy", "vz")})
+    k1, p1 = oi.energies(fin)
+    de = ((k1 + p1) - (k0 + p0)) / -p0
+    assert abs(de) < 1e-6, de
+    assert b.active < b.nsteps * len(ps["m"])
+    b.close()

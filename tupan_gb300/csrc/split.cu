@@ -627,6 +627,12 @@ void split_variant_info(int v, int *ni_per_thread, int *jsplit, int *threads)
     *threads = kVariants[v].threads;
 }
 
+// Kernels with a packed-pair (f32x2) operator: variants 5 and 6 use it.
+bool split_has_x2(int kernel)
+{
+    return kernel == K_PHI || kernel == K_ACC || kernel == K_ACC_JERK;
+}
+
 bool split_supported(int kernel)
 {
     return kernel == K_PHI || kernel == K_ACC || kernel == K_ACC_JERK ||

@@ -112,3 +112,75 @@ class DeviceHermite(object):
             self.close()
         except Exception:
             pass
+
+
+def _declare_block(L):
+    c = ctypes
+    L.tupan_gb300_block_create.argtypes = (
+        [c.c_uint64, c.c_int, c.c_int, c.c_double, c.c_double] + [_DP] * 8
+        + [c.POINTER(c.c_void_p)])
+    L.tupan_gb300_block_create.restype = c.c_int
+    L.tupan_gb300_block_evolve.argtypes = [
+        c.c_void_p, c.c_double, c.c_longlong, _DP, c.POINTER(c.c_longlong),
+        c.POINTER(c.c_longlong)]
+    L.tupan_gb300_block_evolve.restype = c.c_int
+    L.tupan_gb300_block_get_state.argtypes = [c.c_void_p] + [_DP] * 8
+    L.tupan_gb300_block_get_state.restype = c.c_int
+    L.tupan_gb300_block_destroy.argtypes = [c.c_void_p]
+    L.tupan_gb300_block_destroy.restype = c.c_int
+
+
+class DeviceBlockHermite(object):
+    """Hermite (order 4, 6 or 8) with individual power-of-two block steps,
+    device resident; see csrc/blockstep.cu for the scheme."""
+
+    def __init__(self, ps, eta, dt_max, order=4, mode="split"):
+        self.L = lib.load("float64")
+        _declare_block(self.L)
+        self.n = len(ps["m"])
+        arrs = [np.ascontiguousarray(ps[k], dtype=np.float64)
+                for k in ("m", "e2", "rx", "ry", "rz", "vx", "vy", "vz")]
+        h = ctypes.c_void_p()
+        st = self.L.tupan_gb300_block_create(
+            self.n, int(order),
+            lib.MODE_SPLIT if mode == "split" else lib.MODE_EXACT,
+            float(eta), float(dt_max), *[_p(a) for a in arrs],
+            ctypes.byref(h))
+        if st:
+            raise lib.TupanGB300Error("block_create failed: status %d" % st)
+        self.h = h
+        self.time = 0.0
+        self.nsteps = 0
+        self.active = 0
+
+    def evolve(self, t_end, max_steps=0):
+        t = ctypes.c_double()
+        k = ctypes.c_longlong()
+        a = ctypes.c_longlong()
+        st = self.L.tupan_gb300_block_evolve(self.h, float(t_end),
+                                             int(max_steps), ctypes.byref(t),
+                                             ctypes.byref(k), ctypes.byref(a))
+        if st:
+            raise lib.TupanGB300Error("block_evolve failed: status %d" % st)
+        self.time, self.nsteps, self.active = t.value, k.value, a.value
+        return self.time
+
+    def state(self):
+        keys = ("rx", "ry", "rz", "vx", "vy", "vz", "t", "dt")
+        out = {k: np.empty(self.n) for k in keys}
+        st = self.L.tupan_gb300_block_get_state(self.h,
+                                                *[_p(out[k]) for k in keys])
+        if st:
+            raise lib.TupanGB300Error("block_get_state failed")
+        return out
+
+    def close(self):
+        if self.h:
+            self.L.tupan_gb300_block_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
