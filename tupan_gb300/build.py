@@ -32,9 +32,11 @@ UNITS = {
     "abi32.o": ("abi.cu", ["-DTG_ABI_FLOAT32"]),
     "microbench.o": ("microbench.cu", []),
     "driver.o": ("driver.cu", ["-fmad=false"]),
+    "blockstep.o": ("blockstep.cu", ["-fmad=false"]),
 }
 LINKS = {
-    LIB64: ["exact.o", "split.o", "abi64.o", "microbench.o", "driver.o"],
+    LIB64: ["exact.o", "split.o", "abi64.o", "microbench.o", "driver.o",
+            "blockstep.o"],
     LIB32: ["exact.o", "split.o", "abi32.o", "microbench.o"],
 }
 
