@@ -244,6 +244,27 @@ long long tupan_gb300_hermite_tau_log(void *handle, double *out,
 int tupan_gb300_hermite_energy(void *handle, double *ke, double *pe);
 int tupan_gb300_hermite_destroy(void *handle);
 
+/* No counterpart in the reference.  acc_jerk_kernel's arithmetic in SPLIT
+ * mode on DEVICE arrays (argument order of libtupan.h:34-58, then a stream
+ * and an optional host pointer for the error word), for callers that cannot
+ * let the library allocate device memory: an application whose memory
+ * manager owns the whole device heap, or a step loop that must not stall on
+ * cudaMalloc's device-wide synchronisation.  Its scratch (packed particle
+ * records) is a static device array of 6 MiB, so ni and nj are limited to
+ * 65536 each; larger requests return 5 before anything runs.  All calls
+ * share that array: calls that overlap on the GPU race.  The first call on a
+ * device looks up the array's address there; make it outside stream capture.
+ * err_out == NULL: asynchronous; otherwise the call waits for the stream and
+ * stores the sweep's device error word.  Returns 0 or a status code. */
+int tupan_gb300_acc_jerk_split_noalloc(
+    uint64_t ni, const double *im, const double *irx, const double *iry,
+    const double *irz, const double *ie2, const double *ivx,
+    const double *ivy, const double *ivz, uint64_t nj, const double *jm,
+    const double *jrx, const double *jry, const double *jrz,
+    const double *je2, const double *jvx, const double *jvy,
+    const double *jvz, double *iax, double *iay, double *iaz, double *ijx,
+    double *ijy, double *ijz, void *stream, unsigned *err_out);
+
 #ifdef __cplusplus
 }
 #endif

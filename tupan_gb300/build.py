@@ -33,10 +33,11 @@ UNITS = {
     "microbench.o": ("microbench.cu", []),
     "driver.o": ("driver.cu", ["-fmad=false"]),
     "blockstep.o": ("blockstep.cu", ["-fmad=false"]),
+    "noalloc.o": ("noalloc.cu", []),
 }
 LINKS = {
     LIB64: ["exact.o", "split.o", "abi64.o", "microbench.o", "driver.o",
-            "blockstep.o"],
+            "blockstep.o", "noalloc.o"],
     LIB32: ["exact.o", "split.o", "abi32.o", "microbench.o"],
 }
 
