@@ -33,11 +33,15 @@ UNITS = {
     "microbench.o": ("microbench.cu", []),
     "driver.o": ("driver.cu", ["-fmad=false"]),
     "blockstep.o": ("blockstep.cu", ["-fmad=false"]),
+    "sakura.o": ("sakura.cu", ["-fmad=false"]),
+    "mlp.o": ("mlp.cu", []),
+    "ensemble.o": ("ensemble.cu", ["-fmad=false"]),
     "noalloc.o": ("noalloc.cu", []),
 }
 LINKS = {
     LIB64: ["exact.o", "split.o", "abi64.o", "microbench.o", "driver.o",
-            "blockstep.o", "noalloc.o"],
+            "blockstep.o", "sakura.o", "mlp.o", "ensemble.o",
+            "noalloc.o"],
     LIB32: ["exact.o", "split.o", "abi32.o", "microbench.o"],
 }
 

@@ -1,0 +1,547 @@
+// Sakura sweep with the Kepler-branch pairs solved as a separate queue, and
+// a standalone universal-Kepler pair solver with an optional learned start.
+//
+// tupan's sakura_kernel (sakura_kernel.c:33-62) evolves every (i, j) pair as
+// a two-body problem over dt: about 99 % of pairs take the leapfrog branch
+// (r^2 > (64 m / v^2)^2, sakura_kernel_common.h:111-117), the rest the
+// iterative universal-variable solver.  Run inline, one Kepler pair stalls
+// its whole warp.  Here, for the flags the Sakura integrator uses (-1, +1):
+//   1. count, per i, the pairs that take the Kepler branch (cheap test);
+//   2. exclusive scan of the counts;
+//   3. sum the leapfrog pairs in j order and write the Kepler pairs' j
+//      indices, in j order, into each i's segment of a queue;
+//   4. solve the queue, one thread per pair (coherent work);
+//   5. add each i's Kepler contributions, in j order, to its leapfrog sum.
+// The leapfrog branch is bit-identical to the reference (compiled without
+// contraction); the result differs from the reference's interleaved sum only
+// by the order of the additions, and the Kepler branch by CUDA's
+// transcendental functions.
+//
+// The pair solver is also the engine of the learned start: an MLP
+// (4 -> 64 -> 64 -> 1, SiLU, bf16 weights, FP32 accumulation) predicts the
+// ratio of the converged universal anomaly to the plain first guess; the
+// plain Laguerre iteration then runs to the unchanged tolerance.
+
+#include <cuda_bf16.h>
+#include <cuda_runtime.h>
+#include <stdint.h>
+#include <string.h>
+
+#include "tg_common.cuh"
+#include "tg_kepler.cuh"
+
+#define TG_EXPORT extern "C" __attribute__((visibility("default")))
+
+namespace tg {
+
+// ---------------------------------------------------------------------------
+// Learned start: parameters in device memory.
+// ---------------------------------------------------------------------------
+constexpr int MLP_IN = 4, MLP_H = 64;
+
+struct MlpParams {
+    const __nv_bfloat16 *w1;   // MLP_H x MLP_IN
+    const float *b1;           // MLP_H
+    const __nv_bfloat16 *w2;   // MLP_H x MLP_H
+    const float *b2;           // MLP_H
+    const __nv_bfloat16 *w3;   // MLP_H
+    const float *b3;           // 1
+    const float *norm;         // mean[4], 1/std[4] of the features
+};
+
+__device__ __forceinline__ float silu(float x) { return x / (1.0f + __expf(-x)); }
+
+// Features of a single-step solve, from the quantities of kep_setup.
+__device__ __forceinline__ void kep_features(const KepArg<double> &k,
+                                             const double *p, float *f)
+{
+    const double vx = p[3], vy = p[4], vz = p[5];
+    const double v = sqrt(vx * vx + vy * vy + vz * vz);
+    f[0] = (float)log(k.r0);
+    f[1] = (float)log(v > 0 ? v : 1e-300);
+    f[2] = (float)(k.rv0 / (k.r0 * (v > 0 ? v : 1e-300)));
+    f[3] = (float)log(fabs(k.dt) * sqrt(k.m / (k.r0 * k.r0 * k.r0)) + 1e-300);
+}
+
+// Weights are shared by every thread of a block: staged once in shared memory
+// (bf16), activations in registers, FP32 fused multiply-adds.
+struct MlpSmem {
+    __nv_bfloat16 w1[MLP_H * MLP_IN];
+    __nv_bfloat16 w2[MLP_H * MLP_H];
+    __nv_bfloat16 w3[MLP_H];
+    float b1[MLP_H], b2[MLP_H], b3, norm[8];
+};
+
+__device__ void mlp_stage(MlpSmem &S, const MlpParams &P)
+{
+    for (int t = threadIdx.x; t < MLP_H * MLP_H; t += blockDim.x) {
+        S.w2[t] = P.w2[t];
+        if (t < MLP_H * MLP_IN) S.w1[t] = P.w1[t];
+        if (t < MLP_H) {
+            S.w3[t] = P.w3[t];
+            S.b1[t] = P.b1[t];
+            S.b2[t] = P.b2[t];
+        }
+        if (t < 8) S.norm[t] = P.norm[t];
+        if (t == 0) S.b3 = P.b3[0];
+    }
+}
+
+__device__ float mlp_eval(const MlpSmem &S, const float *x_raw)
+{
+    float x[MLP_IN];
+#pragma unroll
+    for (int k = 0; k < MLP_IN; ++k)
+        x[k] = (x_raw[k] - S.norm[k]) * S.norm[4 + k];
+    float h1[MLP_H];
+#pragma unroll
+    for (int o = 0; o < MLP_H; ++o) {
+        float a = S.b1[o];
+#pragma unroll
+        for (int k = 0; k < MLP_IN; ++k)
+            a = __fmaf_rn(__bfloat162float(S.w1[o * MLP_IN + k]), x[k], a);
+        h1[o] = silu(a);
+    }
+    float y = S.b3;
+    for (int o = 0; o < MLP_H; ++o) {
+        float a = S.b2[o];
+#pragma unroll
+        for (int k = 0; k < MLP_H; ++k)
+            a = __fmaf_rn(__bfloat162float(S.w2[o * MLP_H + k]), h1[k], a);
+        y = __fmaf_rn(__bfloat162float(S.w3[o]), silu(a), y);
+    }
+    return y;
+}
+
+// ---------------------------------------------------------------------------
+// Standalone pair solver: one universal_kepler_solver per pair (as the Kepler
+// branch of twobody_solver calls it), optional learned start, optional record
+// of (features, log(root / plain guess)) of each pair's first single-step
+// solve for training.
+// ---------------------------------------------------------------------------
+struct PairSolve {
+    uint64_t n;
+    double dt;
+    const double *m, *e2, *state;   // state: n x 6 (r, v)
+    double *out;                    // n x 6
+    int *iters;                     // Laguerre updates per pair (or null)
+    float *rec_x, *rec_y;           // n x 4 features, n targets (or null)
+    long long budget;
+    int use_mlp;
+    MlpParams mlp;
+};
+
+__global__ void __launch_bounds__(128)
+k_pair_solve(const PairSolve P, unsigned *err)
+{
+    __shared__ MlpSmem S;
+    if (P.use_mlp) mlp_stage(S, P.mlp);
+    __syncthreads();
+    const uint64_t q = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (q >= P.n) return;
+    double p0[6], p1[6];
+    for (int c = 0; c < 6; ++c) p0[c] = P.state[6 * q + c];
+    const double m = P.m[q], e2 = P.e2[q];
+    KepCtx<double> ctx = {0, P.budget, 0, false, false, 0.0};
+    KepArg<double> ka;
+    double s0;
+    const bool moving = kep_setup(P.dt, m, e2, p0, &ka, &s0);
+    if (moving && (P.use_mlp || P.rec_x)) {
+        float f[MLP_IN];
+        kep_features(ka, p0, f);
+        if (P.use_mlp) {
+            const float y = mlp_eval(S, f);
+            ctx.use_start = true;
+            ctx.start = s0 * exp((double)y);
+        }
+        if (P.rec_x) {
+            for (int k = 0; k < MLP_IN; ++k) P.rec_x[4 * q + k] = f[k];
+            double root;
+            int it = 0;
+            const int st = kep_laguerre(s0, &root, ka, &it);
+            P.rec_y[q] = (st == 0 && root / s0 > 0)
+                             ? (float)log(root / s0) : __int_as_float(0x7fc00000);
+        }
+    }
+    kep_solve(P.dt, m, e2, p0, p1, ctx);
+    for (int c = 0; c < 6; ++c) P.out[6 * q + c] = p1[c];
+    if (P.iters) P.iters[q] = (int)ctx.iterations;
+    if (ctx.exhausted) atomicOr(err, (unsigned)DERR_KEPLER_BUDGET);
+}
+
+// ---------------------------------------------------------------------------
+// Queued Sakura sweep (flags -1 and +1).
+// ---------------------------------------------------------------------------
+constexpr int SK_THREADS = 128;
+constexpr int SK_TILE = 128;
+
+struct SakuraArgs {
+    uint64_t ni, nj;
+    const double *ip[8], *jp[8];
+    double *out[6];
+    double dt;
+    long long flag;
+    unsigned *cnt;          // ni (pass 1), then offsets (pass 2)
+    unsigned *queue_j;      // Kepler pairs: j index
+    unsigned *queue_i;      // Kepler pairs: i index
+    double *contrib;        // 6 per queued pair
+    int *iters;             // per queued pair (or null)
+    long long budget;
+    int use_mlp;
+    MlpParams mlp;
+};
+
+// Drift applied before the two-body step for flag -1 (sakura_kernel_common.h
+// :151-157); flag +1 evolves first and drifts after (:158-164).
+__device__ __forceinline__ bool sk_kepler(const double *ip, const double *jp,
+                                          double dt, long long flag,
+                                          double *p0, double *pre, double *m,
+                                          double *e2)
+{
+    pair_state(ip, jp, p0, m, e2);
+    for (int c = 0; c < 6; ++c) pre[c] = p0[c];
+    if (flag == -1) {
+        pre[0] -= pre[3] * dt;
+        pre[1] -= pre[4] * dt;
+        pre[2] -= pre[5] * dt;
+    }
+    return !takes_leapfrog(*m, pre);
+}
+
+template <int PASS>
+__global__ void __launch_bounds__(SK_THREADS)
+k_sakura_pass(const SakuraArgs A)
+{
+    __shared__ double tile[8][SK_TILE];
+    const uint64_t i = (uint64_t)blockIdx.x * SK_THREADS + threadIdx.x;
+    const uint64_t ic = i < A.ni ? i : A.ni - 1;
+    double ip[8];
+    for (int a = 0; a < 8; ++a) ip[a] = A.ip[a][ic];
+    const double dt = A.dt;
+    const long long flag = A.flag;
+    double o[6] = {0, 0, 0, 0, 0, 0};
+    unsigned count = 0;
+    const unsigned base = (PASS == 2 && i < A.ni) ? A.cnt[i] : 0;
+    for (uint64_t j0 = 0; j0 < A.nj; j0 += SK_TILE) {
+        const int n = (int)((A.nj - j0) < SK_TILE ? (A.nj - j0) : SK_TILE);
+        __syncthreads();
+        for (int t = threadIdx.x; t < 8 * SK_TILE; t += SK_THREADS) {
+            const int a = t / SK_TILE, jj = t % SK_TILE;
+            if (jj < n) tile[a][jj] = A.jp[a][j0 + jj];
+        }
+        __syncthreads();
+        for (int jj = 0; jj < n; ++jj) {
+            double jp[8];
+            for (int a = 0; a < 8; ++a) jp[a] = tile[a][jj];
+            double p0[6], pre[6], m, e2;
+            const bool kep = sk_kepler(ip, jp, dt, flag, p0, pre, &m, &e2);
+            if (PASS == 1) {
+                count += kep ? 1u : 0u;
+                continue;
+            }
+            if (kep) {
+                if (i < A.ni) {
+                    A.queue_j[base + count] = (unsigned)(j0 + jj);
+                    A.queue_i[base + count] = (unsigned)i;
+                }
+                ++count;
+                continue;
+            }
+            double p1[6];
+            two_body_leapfrog(dt, m, e2, pre, p1);
+            if (flag == 1) {
+                p1[0] -= p1[3] * dt;
+                p1[1] -= p1[4] * dt;
+                p1[2] -= p1[5] * dt;
+            }
+            const double mu = jp[0] / m;
+            for (int q = 0; q < 6; ++q) o[q] += mu * (p1[q] - p0[q]);
+        }
+    }
+    if (i >= A.ni) return;
+    if (PASS == 1) {
+        A.cnt[i] = count;
+    } else {
+        for (int q = 0; q < 6; ++q) A.out[q][i] = o[q];
+    }
+}
+
+// Exclusive scan of n counts in place (one block; returns the total).
+__global__ void k_scan(unsigned *x, uint64_t n, unsigned long long *total)
+{
+    __shared__ unsigned long long carry;
+    __shared__ unsigned long long part[1024];
+    if (threadIdx.x == 0) carry = 0;
+    __syncthreads();
+    for (uint64_t b = 0; b < n; b += blockDim.x) {
+        const uint64_t i = b + threadIdx.x;
+        unsigned long long v = i < n ? x[i] : 0;
+        part[threadIdx.x] = v;
+        __syncthreads();
+        for (int off = 1; off < (int)blockDim.x; off <<= 1) {
+            unsigned long long t =
+                threadIdx.x >= (unsigned)off ? part[threadIdx.x - off] : 0;
+            __syncthreads();
+            part[threadIdx.x] += t;
+            __syncthreads();
+        }
+        if (i < n) x[i] = (unsigned)(carry + part[threadIdx.x] - v);
+        __syncthreads();
+        if (threadIdx.x == blockDim.x - 1) carry += part[threadIdx.x];
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) *total = carry;
+}
+
+// Step 4: one thread per queued pair.
+__global__ void __launch_bounds__(128)
+k_sakura_kepler(const SakuraArgs A, uint64_t nq, unsigned *err)
+{
+    __shared__ MlpSmem S;
+    if (A.use_mlp) mlp_stage(S, A.mlp);
+    __syncthreads();
+    const uint64_t q = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (q >= nq) return;
+    const uint64_t i = A.queue_i[q], j = A.queue_j[q];
+    double ip[8], jp[8];
+    for (int a = 0; a < 8; ++a) {
+        ip[a] = A.ip[a][i];
+        jp[a] = A.jp[a][j];
+    }
+    double p0[6], pre[6], m, e2, p1[6];
+    sk_kepler(ip, jp, A.dt, A.flag, p0, pre, &m, &e2);
+    KepCtx<double> ctx = {0, A.budget, 0, false, false, 0.0};
+    if (A.use_mlp) {
+        KepArg<double> ka;
+        double s0;
+        if (kep_setup(A.dt, m, e2, pre, &ka, &s0)) {
+            float f[MLP_IN];
+            kep_features(ka, pre, f);
+            ctx.use_start = true;
+            ctx.start = s0 * exp((double)mlp_eval(S, f));
+        }
+    }
+    kep_solve(A.dt, m, e2, pre, p1, ctx);
+    if (A.flag == 1) {
+        p1[0] -= p1[3] * A.dt;
+        p1[1] -= p1[4] * A.dt;
+        p1[2] -= p1[5] * A.dt;
+    }
+    const double mu = jp[0] / m;
+    for (int c = 0; c < 6; ++c) A.contrib[6 * q + c] = mu * (p1[c] - p0[c]);
+    if (A.iters) A.iters[q] = (int)ctx.iterations;
+    if (ctx.exhausted) atomicOr(err, (unsigned)DERR_KEPLER_BUDGET);
+}
+
+// Step 5: add each i's queued contributions in queue (= j) order.
+__global__ void k_sakura_gather(const SakuraArgs A, uint64_t nq)
+{
+    const uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= A.ni) return;
+    const uint64_t b = A.cnt[i];
+    const uint64_t e = (i + 1 < A.ni) ? A.cnt[i + 1] : nq;
+    double o[6];
+    for (int c = 0; c < 6; ++c) o[c] = A.out[c][i];
+    for (uint64_t q = b; q < e; ++q)
+        for (int c = 0; c < 6; ++c) o[c] += A.contrib[6 * q + c];
+    for (int c = 0; c < 6; ++c) A.out[c][i] = o[c];
+}
+
+}  // namespace tg
+
+using namespace tg;
+
+namespace {
+
+struct SakuraWork {
+    unsigned *cnt = nullptr;
+    size_t cnt_cap = 0;
+    unsigned *qi = nullptr, *qj = nullptr;
+    double *contrib = nullptr;
+    int *iters = nullptr;
+    size_t q_cap = 0;
+    unsigned long long *total = nullptr;
+    unsigned *err = nullptr;
+};
+
+SakuraWork g_work;
+MlpParams g_mlp;
+bool g_have_mlp = false;
+
+int grow_queue(size_t nq)
+{
+    if (nq <= g_work.q_cap) return 0;
+    cudaFree(g_work.qi);
+    cudaFree(g_work.qj);
+    cudaFree(g_work.contrib);
+    cudaFree(g_work.iters);
+    size_t cap = nq + nq / 2 + 1024;
+    if (cudaMalloc((void **)&g_work.qi, cap * sizeof(unsigned)) != cudaSuccess ||
+        cudaMalloc((void **)&g_work.qj, cap * sizeof(unsigned)) != cudaSuccess ||
+        cudaMalloc((void **)&g_work.contrib, cap * 6 * sizeof(double)) != cudaSuccess ||
+        cudaMalloc((void **)&g_work.iters, cap * sizeof(int)) != cudaSuccess)
+        return 1;
+    g_work.q_cap = cap;
+    return 0;
+}
+
+}  // namespace
+
+// ===========================================================================
+// C-ABI (no counterpart in the reference).
+// ===========================================================================
+
+// Installs (or, with w1 == NULL, removes) the learned-start network: DEVICE
+// pointers to bf16 weights w1 (64x4), w2 (64x64), w3 (64), fp32 biases b1,
+// b2, b3 and the feature normalisation norm[8] = mean[4], 1/std[4].  The
+// arrays must stay valid while the network is installed.
+TG_EXPORT int tupan_gb300_kepler_set_mlp(const void *w1, const float *b1,
+                                         const void *w2, const float *b2,
+                                         const void *w3, const float *b3,
+                                         const float *norm)
+{
+    if (!w1) {
+        g_have_mlp = false;
+        return ST_OK;
+    }
+    g_mlp.w1 = (const __nv_bfloat16 *)w1;
+    g_mlp.b1 = b1;
+    g_mlp.w2 = (const __nv_bfloat16 *)w2;
+    g_mlp.b2 = b2;
+    g_mlp.w3 = (const __nv_bfloat16 *)w3;
+    g_mlp.b3 = b3;
+    g_mlp.norm = norm;
+    g_have_mlp = true;
+    return ST_OK;
+}
+
+// Solves n independent pairs (DEVICE arrays: m, e2, state n x 6, out n x 6)
+// over dt with universal_kepler_solver's full retry logic; iters, rec_x
+// (n x 4) and rec_y (n) are optional.  use_mlp selects the learned start.
+// Synchronous; returns a status code (3: a solve hit the budget).
+TG_EXPORT int tupan_gb300_kepler_pairs(uint64_t n, double dt, const double *m,
+                                       const double *e2, const double *state,
+                                       double *out, int *iters, float *rec_x,
+                                       float *rec_y, int use_mlp,
+                                       long long budget, void *stream)
+{
+    if (use_mlp && !g_have_mlp) return ST_BAD_ARGUMENT;
+    if (!g_work.err && cudaMalloc((void **)&g_work.err, sizeof(unsigned)) !=
+                           cudaSuccess)
+        return ST_CUDA;
+    cudaStream_t st = (cudaStream_t)stream;
+    cudaMemsetAsync(g_work.err, 0, sizeof(unsigned), st);
+    PairSolve P;
+    memset(&P, 0, sizeof(P));
+    P.n = n;
+    P.dt = dt;
+    P.m = m;
+    P.e2 = e2;
+    P.state = state;
+    P.out = out;
+    P.iters = iters;
+    P.rec_x = rec_x;
+    P.rec_y = rec_y;
+    P.budget = budget > 0 ? budget : (1LL << 20);
+    P.use_mlp = use_mlp;
+    P.mlp = g_mlp;
+    if (n) {
+        k_pair_solve<<<(unsigned)((n + 127) / 128), 128, 0, st>>>(P, g_work.err);
+        g_launch_count += 1;
+    }
+    unsigned h = 0;
+    if (cudaMemcpyAsync(&h, g_work.err, sizeof(unsigned),
+                        cudaMemcpyDeviceToHost, st) != cudaSuccess ||
+        cudaStreamSynchronize(st) != cudaSuccess)
+        return ST_CUDA;
+    return h ? ST_DEVICE : ST_OK;
+}
+
+// sakura_kernel (libtupan.h:203-229) on DEVICE arrays with the Kepler-branch
+// pairs solved as a queue; flag must be -1 or +1 (the integrator's flags).
+// i_attrs/j_attrs: 8 device pointers each (m r e2 v); outs: 6.  Optional
+// iteration histogram: kepler_iters (host, 65 bins; bin k counts solves with
+// k Laguerre updates, the last bin k >= 64).  Returns the number of queued
+// (Kepler-branch) pairs in *n_kepler.  Synchronous.
+TG_EXPORT int tupan_gb300_sakura_queue(uint64_t ni, const void *const *i_attrs,
+                                       uint64_t nj, const void *const *j_attrs,
+                                       double dt, int64_t flag,
+                                       void *const *outs, int use_mlp,
+                                       long long budget, void *stream,
+                                       unsigned long long *n_kepler,
+                                       long long *kepler_iters)
+{
+    if (flag != -1 && flag != 1) return ST_BAD_ARGUMENT;
+    if (use_mlp && !g_have_mlp) return ST_BAD_ARGUMENT;
+    if (ni == 0) return ST_OK;
+    cudaStream_t st = (cudaStream_t)stream;
+    if (!g_work.err && (cudaMalloc((void **)&g_work.err, sizeof(unsigned)) !=
+                            cudaSuccess))
+        return ST_CUDA;
+    if (!g_work.total &&
+        cudaMalloc((void **)&g_work.total, sizeof(unsigned long long)) !=
+            cudaSuccess)
+        return ST_CUDA;
+    if (ni > g_work.cnt_cap) {
+        cudaFree(g_work.cnt);
+        if (cudaMalloc((void **)&g_work.cnt, ni * sizeof(unsigned)) != cudaSuccess)
+            return ST_CUDA;
+        g_work.cnt_cap = ni;
+    }
+    SakuraArgs A;
+    memset(&A, 0, sizeof(A));
+    A.ni = ni;
+    A.nj = nj;
+    for (int a = 0; a < 8; ++a) {
+        A.ip[a] = (const double *)i_attrs[a];
+        A.jp[a] = (const double *)j_attrs[a];
+    }
+    for (int c = 0; c < 6; ++c) A.out[c] = (double *)outs[c];
+    A.dt = dt;
+    A.flag = flag;
+    A.cnt = g_work.cnt;
+    A.budget = budget > 0 ? budget : (1LL << 20);
+    A.use_mlp = use_mlp;
+    A.mlp = g_mlp;
+    cudaMemsetAsync(g_work.err, 0, sizeof(unsigned), st);
+    const unsigned blocks = (unsigned)((ni + SK_THREADS - 1) / SK_THREADS);
+    k_sakura_pass<1><<<blocks, SK_THREADS, 0, st>>>(A);
+    k_scan<<<1, 1024, 0, st>>>(g_work.cnt, ni, g_work.total);
+    g_launch_count += 2;
+    unsigned long long nq = 0;
+    if (cudaMemcpyAsync(&nq, g_work.total, sizeof(nq), cudaMemcpyDeviceToHost,
+                        st) != cudaSuccess ||
+        cudaStreamSynchronize(st) != cudaSuccess)
+        return ST_CUDA;
+    if (grow_queue(nq ? nq : 1)) return ST_CUDA;
+    A.queue_i = g_work.qi;
+    A.queue_j = g_work.qj;
+    A.contrib = g_work.contrib;
+    A.iters = kepler_iters ? g_work.iters : nullptr;
+    k_sakura_pass<2><<<blocks, SK_THREADS, 0, st>>>(A);
+    g_launch_count += 1;
+    if (nq) {
+        k_sakura_kepler<<<(unsigned)((nq + 127) / 128), 128, 0, st>>>(
+            A, nq, g_work.err);
+        k_sakura_gather<<<(unsigned)((ni + 127) / 128), 128, 0, st>>>(A, nq);
+        g_launch_count += 2;
+    }
+    unsigned h = 0;
+    if (cudaMemcpyAsync(&h, g_work.err, sizeof(unsigned),
+                        cudaMemcpyDeviceToHost, st) != cudaSuccess ||
+        cudaStreamSynchronize(st) != cudaSuccess)
+        return ST_CUDA;
+    if (n_kepler) *n_kepler = nq;
+    if (kepler_iters) {
+        for (int k = 0; k < 65; ++k) kepler_iters[k] = 0;
+        if (nq) {
+            int *hi = (int *)malloc(nq * sizeof(int));
+            if (!hi) return ST_CUDA;
+            cudaMemcpy(hi, g_work.iters, nq * sizeof(int), cudaMemcpyDeviceToHost);
+            for (unsigned long long q = 0; q < nq; ++q)
+                kepler_iters[hi[q] < 64 ? hi[q] : 64] += 1;
+            free(hi);
+        }
+    }
+    return h ? ST_DEVICE : ST_OK;
+}

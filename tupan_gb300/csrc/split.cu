@@ -599,6 +599,153 @@ __global__ void split_finalize(const SplitLaunch L, int gsplit)
     }
 }
 
+
+// ---------------------------------------------------------------------------
+// Batched sweep over an ensemble of independent systems (one persistent
+// launch).  System s owns particles [off[s], off[s+1]); each i interacts only
+// with the j of its own system.  CTAs take systems from an atomic work queue
+// (largest first, by the host-sorted order), stage the system's packed
+// records in shared memory with one bulk copy per tile, and give each i
+// `lanes` threads (a power of two chosen from the system size) that split
+// the j loop and combine through shuffles.  Systems whose `active` flag is 0
+// are skipped.
+// ---------------------------------------------------------------------------
+struct BatchLaunch {
+    const float4 *rec;        // packed records of all systems
+    const uint64_t *off;      // n_sys + 1 offsets
+    const unsigned *order;    // systems in processing order
+    const int *active;        // per system (may be null: all active)
+    unsigned n_sys;
+    unsigned *queue;          // work counter (zeroed before the launch)
+    double *out[MAX_OUT];
+    float eta;
+    double eta_d;
+    unsigned *err;
+};
+
+constexpr int BATCH_NT = 256;
+constexpr int BATCH_MAXN = 512;           // largest system held in smem
+
+template <class Op>
+__global__ void __launch_bounds__(BATCH_NT, 2)
+split_sweep_batched(const BatchLaunch L)
+{
+    constexpr int NF = Op::NF, NO = Op::NO, MAXC = Op::MAXC;
+    __shared__ __align__(128) float4 rec[BATCH_MAXN * NF];
+    __shared__ __align__(8) uint64_t bar;
+    __shared__ unsigned item;
+    const int tid = threadIdx.x;
+    if (tid == 0) {
+        mbar_init(&bar, 1);
+        mbar_init_fence();
+    }
+    __syncthreads();
+    uint32_t phase = 0;
+    for (;;) {
+        if (tid == 0) item = atomicAdd(L.queue, 1u);
+        __syncthreads();
+        const unsigned w = item;
+        if (w >= L.n_sys) break;
+        const unsigned sys = L.order[w];
+        if (L.active && !L.active[sys]) {
+            __syncthreads();
+            continue;
+        }
+        const uint64_t b = L.off[sys];
+        const int n = (int)(L.off[sys + 1] - b);
+        if (n > BATCH_MAXN) {
+            if (tid == 0) atomicOr(L.err, (unsigned)DERR_BAD_LAUNCH);
+            __syncthreads();
+            continue;
+        }
+        if (tid == 0 && n > 0) {
+            const uint32_t bytes = (uint32_t)(n * NF * sizeof(float4));
+            mbar_arrive_expect_tx(&bar, bytes);
+            bulk_g2s(rec, L.rec + b * NF, bytes, &bar);
+        }
+        bool got = n > 0 ? mbar_wait_bounded(&bar, phase, L.err) : true;
+        if (n > 0) phase ^= 1u;
+        if (!__syncthreads_and(got)) break;
+        // lanes per i: enough to occupy the block, at most 32
+        int lanes = 1;
+        while (lanes < 32 && lanes * 2 * n <= BATCH_NT) lanes *= 2;
+        const int groups = BATCH_NT / lanes;
+        const int lane = tid % lanes;
+        for (int i0 = tid / lanes; i0 - tid / lanes < n; i0 += groups) {
+            const int i = i0 < n ? i0 : n - 1;
+            const typename Op::P ip = Op::load(rec + i * NF);
+            float sum[NO], corr[NO], part[NO];
+#pragma unroll
+            for (int c = 0; c < NO; ++c) sum[c] = corr[c] = part[c] = 0.f;
+            int cnt = 0;
+            for (int j = lane; j < n; j += lanes) {
+                const typename Op::P jp = Op::load(rec + j * NF);
+                Op::pair(ip, jp, part, L.eta);
+                if (++cnt == 16) {
+#pragma unroll
+                    for (int c = 0; c < NO; ++c) {
+                        if (c == MAXC) sum[c] = fmaxf(sum[c], part[c]);
+                        else kahan_add(sum[c], corr[c], part[c]);
+                        part[c] = 0.f;
+                    }
+                    cnt = 0;
+                }
+            }
+            double v[NO];
+#pragma unroll
+            for (int c = 0; c < NO; ++c) {
+                if (c == MAXC) sum[c] = fmaxf(sum[c], part[c]);
+                else kahan_add(sum[c], corr[c], part[c]);
+                v[c] = (c == MAXC) ? (double)sum[c]
+                                   : (double)sum[c] - (double)corr[c];
+                for (int o = lanes / 2; o > 0; o >>= 1) {
+                    double u = __shfl_xor_sync(0xffffffffu, v[c], o, lanes);
+                    v[c] = (c == MAXC) ? fmax(v[c], u) : v[c] + u;
+                }
+            }
+            if (lane == 0 && i0 < n) {
+                Op::finish(v, L.eta_d);
+#pragma unroll
+                for (int c = 0; c < NO; ++c) L.out[c][b + i] = v[c];
+            }
+        }
+        __syncthreads();   // the records of this system are no longer read
+    }
+}
+
+cudaError_t launch_split_batched(int kernel, const float4 *rec,
+                                 const uint64_t *off, const unsigned *order,
+                                 const int *active, unsigned n_sys,
+                                 unsigned *queue, void *const *out, double eta,
+                                 unsigned *err, int sms, cudaStream_t st)
+{
+    BatchLaunch L;
+    L.rec = rec;
+    L.off = off;
+    L.order = order;
+    L.active = active;
+    L.n_sys = n_sys;
+    L.queue = queue;
+    for (int c = 0; c < MAX_OUT; ++c)
+        L.out[c] = c < n_out(kernel) ? (double *)out[c] : nullptr;
+    L.eta = (float)eta;
+    L.eta_d = eta;
+    L.err = err;
+    cudaError_t e = cudaMemsetAsync(queue, 0, sizeof(unsigned), st);
+    if (e != cudaSuccess) return e;
+    const unsigned grid = (unsigned)(sms * 2 < (int)n_sys ? sms * 2 : n_sys);
+    if (grid == 0) return cudaSuccess;
+    switch (kernel) {
+    case K_ACC: split_sweep_batched<AccS><<<grid, BATCH_NT, 0, st>>>(L); break;
+    case K_ACC_JERK: split_sweep_batched<AccJerkS><<<grid, BATCH_NT, 0, st>>>(L); break;
+    case K_TSTEP: split_sweep_batched<TstepS><<<grid, BATCH_NT, 0, st>>>(L); break;
+    case K_PHI: split_sweep_batched<PhiS><<<grid, BATCH_NT, 0, st>>>(L); break;
+    default: return cudaErrorInvalidValue;
+    }
+    g_launch_count += 1;
+    return cudaGetLastError();
+}
+
 // ---------------------------------------------------------------------------
 // Variant table and launcher.
 // ---------------------------------------------------------------------------

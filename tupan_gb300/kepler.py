@@ -1,0 +1,80 @@
+"""Sakura sweep with queued Kepler-branch pairs, the batched pair solver and
+the learned start (device arrays given as torch tensors or raw pointers)."""
+
+import ctypes
+
+import numpy as np
+
+from . import lib
+
+_VP = ctypes.c_void_p
+
+
+def _declare(L):
+    c = ctypes
+    L.tupan_gb300_kepler_set_mlp.argtypes = [_VP] * 7
+    L.tupan_gb300_kepler_set_mlp.restype = c.c_int
+    L.tupan_gb300_kepler_pairs.argtypes = [
+        c.c_uint64, c.c_double, _VP, _VP, _VP, _VP, _VP, _VP, _VP, c.c_int,
+        c.c_longlong, _VP]
+    L.tupan_gb300_kepler_pairs.restype = c.c_int
+    L.tupan_gb300_sakura_queue.argtypes = [
+        c.c_uint64, c.POINTER(_VP), c.c_uint64, c.POINTER(_VP), c.c_double,
+        c.c_int64, c.POINTER(_VP), c.c_int, c.c_longlong, _VP,
+        c.POINTER(c.c_ulonglong), c.POINTER(c.c_longlong)]
+    L.tupan_gb300_sakura_queue.restype = c.c_int
+
+
+def _lib():
+    L = lib.load("float64")
+    if not getattr(L, "_kepler_declared", False):
+        _declare(L)
+        L._kepler_declared = True
+    return L
+
+
+def _ptr(t):
+    return None if t is None else t.data_ptr()
+
+
+def sakura_queue(ni, i_ptrs, nj, j_ptrs, out_ptrs, dt, flag, use_mlp=False,
+                 budget=0, stream=None, histogram=False):
+    """sakura_kernel over device arrays (flag -1 or +1).  Returns the number
+    of Kepler-branch pairs and, if asked, the Laguerre-update histogram."""
+    L = _lib()
+    ia = (_VP * 8)(*i_ptrs)
+    ja = (_VP * 8)(*j_ptrs)
+    oa = (_VP * 6)(*out_ptrs)
+    nk = ctypes.c_ulonglong()
+    hist = (ctypes.c_longlong * 65)() if histogram else None
+    st = L.tupan_gb300_sakura_queue(int(ni), ia, int(nj), ja, float(dt),
+                                    int(flag), oa, 1 if use_mlp else 0,
+                                    int(budget), stream, ctypes.byref(nk),
+                                    hist)
+    if st:
+        raise lib.TupanGB300Error("sakura_queue failed: status %d" % st)
+    return nk.value, (np.array(hist[:]) if histogram else None)
+
+
+def kepler_pairs(n, dt, m, e2, state, out, iters=None, rec_x=None,
+                 rec_y=None, use_mlp=False, budget=0, stream=None):
+    """Solve n pairs (device tensors); see tupan_gb300_kepler_pairs."""
+    st = _lib().tupan_gb300_kepler_pairs(
+        int(n), float(dt), _ptr(m), _ptr(e2), _ptr(state), _ptr(out),
+        _ptr(iters), _ptr(rec_x), _ptr(rec_y), 1 if use_mlp else 0,
+        int(budget), stream)
+    if st:
+        raise lib.TupanGB300Error("kepler_pairs failed: status %d" % st)
+
+
+def set_mlp(w1, b1, w2, b2, w3, b3, norm):
+    """Install the learned start (device tensors; bf16 weights)."""
+    st = _lib().tupan_gb300_kepler_set_mlp(*[_ptr(t) for t in
+                                             (w1, b1, w2, b2, w3, b3, norm)])
+    if st:
+        raise lib.TupanGB300Error("set_mlp failed")
+
+
+def clear_mlp():
+    _lib().tupan_gb300_kepler_set_mlp(None, None, None, None, None, None,
+                                      None)
