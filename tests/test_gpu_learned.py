@@ -14,7 +14,7 @@ def test_mlp_gradient_matches_oracle():
     from tupan_gb300.learned import LearnedStart
     rng = np.random.default_rng(4)
     n = 1000
-    X = rng.normal(size=(n, 4)).astype(np.float32) * [1, 2, 0.5, 3]
+    X = (rng.normal(size=(n, 4)) * [1, 2, 0.5, 3]).astype(np.float32)
     Y = rng.normal(size=n).astype(np.float32)
     Y[::97] = np.nan                       # failed solves carry no loss
     net = LearnedStart(seed=3)
@@ -32,25 +32,39 @@ def test_mlp_gradient_matches_oracle():
     assert np.max(np.abs(g_gpu - g_ref)[big] / np.abs(g_ref)[big]) < 1e-3
 
 
-def test_training_and_learned_start_keep_converged_states():
-    torch = pytest.importorskip("torch")
-    from tupan_gb300 import kepler as kp
-    from tupan_gb300.learned import LearnedStart, evaluate, training_set
-    dt = 1.0 / 8
-    X, Y = training_set(dts=(dt,), seeds=range(1, 3), n_bodies=2048)
+def test_training_reduces_loss():
+    pytest.importorskip("torch")
+    from tupan_gb300.learned import LearnedStart, training_set
+    X, Y, _ = training_set(dts=(1.0 / 8,), seeds=(1,), n_bodies=2048)
     ok = np.isfinite(Y)
     assert ok.mean() > 0.99
     net = LearnedStart(seed=1)
-    hist = net.fit(X[ok], Y[ok], epochs=8, batch=4096)
-    assert hist[-1] < 0.5 * hist[0]
+    hist = net.fit(X[ok], Y[ok], epochs=6, batch=4096)
+    assert hist[-1] < 0.6 * hist[0], hist
+
+
+def test_trained_start_keeps_states_and_cuts_the_iteration_tail():
+    """What the trained network (trained on the GPU by
+    `python -m tupan_gb300.learned`, shipped as kepler_start.npz) gains over
+    the plain first guess dt/r: converged states are unchanged (same
+    stopping rule), and where the plain guess needs more than two Laguerre
+    updates (larger dt) the mean count and the tail of long solves drop.  At
+    dt = 1/512 both need the minimum of two updates for >99% of pairs."""
+    pytest.importorskip("torch")
+    from tupan_gb300 import kepler as kp
+    from tupan_gb300.learned import LearnedStart, evaluate
+    net = LearnedStart.load()
     net.install()
     try:
-        r = evaluate(net, dt, seeds=(77,), n_bodies=2048)
+        big = evaluate(net, 1.0 / 8, seeds=(77,), n_bodies=2048)
+        small = evaluate(net, 1.0 / 512, seeds=(77,), n_bodies=2048)
     finally:
         kp.clear_mlp()
-    print(r)
-    # the stopping rule is unchanged: converged states agree to round-off
-    assert r["max_state_diff_rel"] <= 1e-11
-    # and the learned start does not cost iterations where the plain guess
-    # already needs more than the minimum of two
-    assert r["mean_iters_learned"] <= r["mean_iters_plain"]
+    print(big)
+    print(small)
+    for r in (big, small):
+        assert r["max_state_diff_rel"] <= 1e-11
+    tail = lambda h: sum(h[5:])
+    assert big["mean_iters_learned"] < big["mean_iters_plain"]
+    assert tail(big["hist_learned"]) < 0.5 * tail(big["hist_plain"])
+    assert small["mean_iters_learned"] <= small["mean_iters_plain"] + 0.01

@@ -47,6 +47,7 @@ struct MlpParams {
     const __nv_bfloat16 *w3;   // MLP_H
     const float *b3;           // 1
     const float *norm;         // mean[4], 1/std[4] of the features
+    float gate;                // learned start only where feature 3 exceeds it
 };
 
 __device__ __forceinline__ float silu(float x) { return x / (1.0f + __expf(-x)); }
@@ -149,7 +150,7 @@ k_pair_solve(const PairSolve P, unsigned *err)
     if (moving && (P.use_mlp || P.rec_x)) {
         float f[MLP_IN];
         kep_features(ka, p0, f);
-        if (P.use_mlp) {
+        if (P.use_mlp && f[3] > P.mlp.gate) {
             const float y = mlp_eval(S, f);
             ctx.use_start = true;
             ctx.start = s0 * exp((double)y);
@@ -317,8 +318,10 @@ k_sakura_kepler(const SakuraArgs A, uint64_t nq, unsigned *err)
         if (kep_setup(A.dt, m, e2, pre, &ka, &s0)) {
             float f[MLP_IN];
             kep_features(ka, pre, f);
-            ctx.use_start = true;
-            ctx.start = s0 * exp((double)mlp_eval(S, f));
+            if (f[3] > A.mlp.gate) {
+                ctx.use_start = true;
+                ctx.start = s0 * exp((double)mlp_eval(S, f));
+            }
         }
     }
     kep_solve(A.dt, m, e2, pre, p1, ctx);
@@ -394,11 +397,14 @@ int grow_queue(size_t nq)
 // Installs (or, with w1 == NULL, removes) the learned-start network: DEVICE
 // pointers to bf16 weights w1 (64x4), w2 (64x64), w3 (64), fp32 biases b1,
 // b2, b3 and the feature normalisation norm[8] = mean[4], 1/std[4].  The
-// arrays must stay valid while the network is installed.
+// network is evaluated only for solves whose feature log(|dt| sqrt(m/r^3))
+// exceeds `gate` (where the plain guess needs more than the minimum two
+// updates); elsewhere the plain guess is kept.  The arrays must stay valid
+// while the network is installed.
 TG_EXPORT int tupan_gb300_kepler_set_mlp(const void *w1, const float *b1,
                                          const void *w2, const float *b2,
                                          const void *w3, const float *b3,
-                                         const float *norm)
+                                         const float *norm, float gate)
 {
     if (!w1) {
         g_have_mlp = false;
@@ -411,6 +417,7 @@ TG_EXPORT int tupan_gb300_kepler_set_mlp(const void *w1, const float *b1,
     g_mlp.w3 = (const __nv_bfloat16 *)w3;
     g_mlp.b3 = b3;
     g_mlp.norm = norm;
+    g_mlp.gate = gate;
     g_have_mlp = true;
     return ST_OK;
 }
@@ -544,4 +551,149 @@ TG_EXPORT int tupan_gb300_sakura_queue(uint64_t ni, const void *const *i_attrs,
         }
     }
     return h ? ST_DEVICE : ST_OK;
+}
+
+// ===========================================================================
+// Device-resident Sakura integrator (sakura.py:22-50, fixed step): per step
+// drift tau/2, queued Sakura sweeps with flag -1 then +1 at dt = tau/2, each
+// followed by r += dr, v += dv, and a final drift tau/2.  State in HBM.
+// ===========================================================================
+namespace {
+
+__global__ void k_drift(double *r0, double *r1, double *r2, const double *v0,
+                        const double *v1, const double *v2, uint64_t n,
+                        double tau)
+{
+    for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n;
+         i += (uint64_t)gridDim.x * blockDim.x) {
+        r0[i] = r0[i] + v0[i] * tau / 2;
+        r1[i] = r1[i] + v1[i] * tau / 2;
+        r2[i] = r2[i] + v2[i] * tau / 2;
+    }
+}
+
+__global__ void k_kick(double *const *x, const double *const *d, uint64_t n)
+{
+    for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n;
+         i += (uint64_t)gridDim.x * blockDim.x)
+        for (int c = 0; c < 6; ++c) x[c][i] = x[c][i] + d[c][i];
+}
+
+struct SakuraSys {
+    uint64_t n = 0;
+    double *pool = nullptr;          // m e2 r3 v3 d6
+    double *a[8];                    // m r(3) e2 v(3), the kernels' order
+    double *d[6];
+    double **xd = nullptr, **dd = nullptr;   // device arrays of pointers
+    cudaStream_t stream = nullptr;
+    int use_mlp = 0;
+    long long kepler_total = 0, steps = 0;
+    long long hist[65] = {0};
+    double t = 0.0;
+};
+
+}  // namespace
+
+TG_EXPORT int tupan_gb300_sakura_create(uint64_t n, const double *m,
+                                        const double *e2, const double *rx,
+                                        const double *ry, const double *rz,
+                                        const double *vx, const double *vy,
+                                        const double *vz, void **handle)
+{
+    if (!handle || n == 0) return ST_BAD_ARGUMENT;
+    SakuraSys *S = new SakuraSys();
+    S->n = n;
+    if (cudaStreamCreateWithFlags(&S->stream, cudaStreamNonBlocking) !=
+            cudaSuccess ||
+        cudaMalloc((void **)&S->pool, 14 * n * sizeof(double)) != cudaSuccess ||
+        cudaMalloc((void **)&S->xd, 6 * sizeof(double *)) != cudaSuccess ||
+        cudaMalloc((void **)&S->dd, 6 * sizeof(double *)) != cudaSuccess)
+        return ST_CUDA;
+    for (int k = 0; k < 8; ++k) S->a[k] = S->pool + (size_t)k * n;
+    for (int k = 0; k < 6; ++k) S->d[k] = S->pool + (size_t)(8 + k) * n;
+    const double *src[8] = {m, rx, ry, rz, e2, vx, vy, vz};
+    for (int k = 0; k < 8; ++k)
+        if (cudaMemcpy(S->a[k], src[k], n * sizeof(double),
+                       cudaMemcpyHostToDevice) != cudaSuccess)
+            return ST_CUDA;
+    double *xs[6] = {S->a[1], S->a[2], S->a[3], S->a[5], S->a[6], S->a[7]};
+    cudaMemcpy(S->xd, xs, sizeof(xs), cudaMemcpyHostToDevice);
+    cudaMemcpy(S->dd, S->d, sizeof(S->d), cudaMemcpyHostToDevice);
+    *handle = S;
+    return ST_OK;
+}
+
+// Fixed-step Sakura steps of size tau until t >= t_end (t_end - t a multiple
+// of tau is the intended use).  use_mlp: learned Kepler start.  kepler_iters
+// (host, 65 bins) accumulates the Laguerre-update histogram if not NULL.
+TG_EXPORT int tupan_gb300_sakura_evolve(void *handle, double tau, double t_end,
+                                        int use_mlp, double *t_out,
+                                        long long *steps_out,
+                                        long long *kepler_out,
+                                        long long *kepler_iters)
+{
+    SakuraSys *S = (SakuraSys *)handle;
+    if (!S || !(tau > 0)) return ST_BAD_ARGUMENT;
+    const uint64_t n = S->n;
+    const unsigned g = (unsigned)((n + 255) / 256 < 1216 ? (n + 255) / 256 : 1216);
+    void *ia[8];
+    for (int k = 0; k < 8; ++k) ia[k] = S->a[k];
+    void *oa[6];
+    for (int k = 0; k < 6; ++k) oa[k] = S->d[k];
+    long long h[65];
+    while (S->t < t_end) {
+        k_drift<<<g, 256, 0, S->stream>>>(S->a[1], S->a[2], S->a[3], S->a[5],
+                                          S->a[6], S->a[7], n, tau);
+        g_launch_count += 1;
+        for (int flag = -1; flag <= 1; flag += 2) {
+            unsigned long long nk = 0;
+            int st = tupan_gb300_sakura_queue(n, ia, n, ia, tau / 2, flag, oa,
+                                              use_mlp, 0, S->stream, &nk,
+                                              kepler_iters ? h : nullptr);
+            if (st) return st;
+            S->kepler_total += (long long)nk;
+            if (kepler_iters)
+                for (int k = 0; k < 65; ++k) kepler_iters[k] += h[k];
+            k_kick<<<g, 256, 0, S->stream>>>(S->xd, S->dd, n);
+            g_launch_count += 1;
+        }
+        k_drift<<<g, 256, 0, S->stream>>>(S->a[1], S->a[2], S->a[3], S->a[5],
+                                          S->a[6], S->a[7], n, tau);
+        g_launch_count += 1;
+        S->t += tau;
+        S->steps += 1;
+    }
+    if (cudaStreamSynchronize(S->stream) != cudaSuccess) return ST_CUDA;
+    if (t_out) *t_out = S->t;
+    if (steps_out) *steps_out = S->steps;
+    if (kepler_out) *kepler_out = S->kepler_total;
+    return ST_OK;
+}
+
+TG_EXPORT int tupan_gb300_sakura_get_state(void *handle, double *rx,
+                                           double *ry, double *rz, double *vx,
+                                           double *vy, double *vz)
+{
+    SakuraSys *S = (SakuraSys *)handle;
+    if (!S) return ST_BAD_ARGUMENT;
+    double *dst[6] = {rx, ry, rz, vx, vy, vz};
+    double *src[6] = {S->a[1], S->a[2], S->a[3], S->a[5], S->a[6], S->a[7]};
+    for (int k = 0; k < 6; ++k)
+        if (cudaMemcpy(dst[k], src[k], S->n * sizeof(double),
+                       cudaMemcpyDeviceToHost) != cudaSuccess)
+            return ST_CUDA;
+    return ST_OK;
+}
+
+TG_EXPORT int tupan_gb300_sakura_destroy(void *handle)
+{
+    SakuraSys *S = (SakuraSys *)handle;
+    if (!S) return ST_BAD_ARGUMENT;
+    cudaStreamSynchronize(S->stream);
+    cudaFree(S->pool);
+    cudaFree(S->xd);
+    cudaFree(S->dd);
+    cudaStreamDestroy(S->stream);
+    delete S;
+    return ST_OK;
 }

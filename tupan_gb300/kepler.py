@@ -12,7 +12,7 @@ _VP = ctypes.c_void_p
 
 def _declare(L):
     c = ctypes
-    L.tupan_gb300_kepler_set_mlp.argtypes = [_VP] * 7
+    L.tupan_gb300_kepler_set_mlp.argtypes = [_VP] * 7 + [c.c_float]
     L.tupan_gb300_kepler_set_mlp.restype = c.c_int
     L.tupan_gb300_kepler_pairs.argtypes = [
         c.c_uint64, c.c_double, _VP, _VP, _VP, _VP, _VP, _VP, _VP, c.c_int,
@@ -67,14 +67,88 @@ def kepler_pairs(n, dt, m, e2, state, out, iters=None, rec_x=None,
         raise lib.TupanGB300Error("kepler_pairs failed: status %d" % st)
 
 
-def set_mlp(w1, b1, w2, b2, w3, b3, norm):
-    """Install the learned start (device tensors; bf16 weights)."""
+def set_mlp(w1, b1, w2, b2, w3, b3, norm, gate=float("-inf")):
+    """Install the learned start (device tensors; bf16 weights), used where
+    log(|dt| sqrt(m / r^3)) > gate."""
     st = _lib().tupan_gb300_kepler_set_mlp(*[_ptr(t) for t in
-                                             (w1, b1, w2, b2, w3, b3, norm)])
+                                             (w1, b1, w2, b2, w3, b3, norm)],
+                                           float(gate))
     if st:
         raise lib.TupanGB300Error("set_mlp failed")
 
 
 def clear_mlp():
     _lib().tupan_gb300_kepler_set_mlp(None, None, None, None, None, None,
-                                      None)
+                                      None, 0.0)
+
+
+_DP = ctypes.POINTER(ctypes.c_double)
+
+
+class DeviceSakura(object):
+    """Fixed-step Sakura integrator (tupan/integrator/sakura.py:22-50) with
+    the particles resident on the GPU and queued Kepler-branch solves."""
+
+    KEYS = ("m", "e2", "rx", "ry", "rz", "vx", "vy", "vz")
+
+    def __init__(self, ps):
+        L = _lib()
+        c = ctypes
+        L.tupan_gb300_sakura_create.argtypes = [c.c_uint64] + [_DP] * 8 + [
+            c.POINTER(_VP)]
+        L.tupan_gb300_sakura_create.restype = c.c_int
+        L.tupan_gb300_sakura_evolve.argtypes = [
+            _VP, c.c_double, c.c_double, c.c_int, _DP,
+            c.POINTER(c.c_longlong), c.POINTER(c.c_longlong),
+            c.POINTER(c.c_longlong)]
+        L.tupan_gb300_sakura_evolve.restype = c.c_int
+        L.tupan_gb300_sakura_get_state.argtypes = [_VP] + [_DP] * 6
+        L.tupan_gb300_sakura_get_state.restype = c.c_int
+        L.tupan_gb300_sakura_destroy.argtypes = [_VP]
+        L.tupan_gb300_sakura_destroy.restype = c.c_int
+        self.L = L
+        self.n = len(ps["m"])
+        arrs = [np.ascontiguousarray(ps[k], dtype=np.float64)
+                for k in self.KEYS]
+        h = _VP()
+        st = L.tupan_gb300_sakura_create(self.n,
+                                         *[a.ctypes.data_as(_DP) for a in arrs],
+                                         ctypes.byref(h))
+        if st:
+            raise lib.TupanGB300Error("sakura_create failed: status %d" % st)
+        self.h = h
+        self.hist = np.zeros(65, np.int64)
+
+    def evolve(self, tau, t_end, use_mlp=False):
+        t = ctypes.c_double()
+        k = ctypes.c_longlong()
+        nk = ctypes.c_longlong()
+        h = (ctypes.c_longlong * 65)()
+        st = self.L.tupan_gb300_sakura_evolve(self.h, float(tau), float(t_end),
+                                              1 if use_mlp else 0,
+                                              ctypes.byref(t), ctypes.byref(k),
+                                              ctypes.byref(nk), h)
+        if st:
+            raise lib.TupanGB300Error("sakura_evolve failed: status %d" % st)
+        self.hist += np.array(h[:])
+        return t.value, k.value, nk.value
+
+    def state(self):
+        out = {c: np.empty(self.n) for c in ("rx", "ry", "rz", "vx", "vy", "vz")}
+        st = self.L.tupan_gb300_sakura_get_state(
+            self.h, *[out[c].ctypes.data_as(_DP)
+                      for c in ("rx", "ry", "rz", "vx", "vy", "vz")])
+        if st:
+            raise lib.TupanGB300Error("sakura_get_state failed")
+        return out
+
+    def close(self):
+        if self.h:
+            self.L.tupan_gb300_sakura_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

@@ -106,6 +106,7 @@ class LearnedStart(object):
         self.norm[4:] = 1.0
         bf = lambda n: torch.zeros(n, dtype=torch.bfloat16, device=dev)
         self.w1, self.w2, self.w3 = bf(H * IN), bf(H * H), bf(H)
+        self.gate = float("-inf")
         self.steps = 0
         self._round()
 
@@ -183,11 +184,27 @@ class LearnedStart(object):
         self._b3 = self.rw[N_PARAM - 1:N_PARAM].contiguous()
         self._b1 = b1
         kp.set_mlp(self.w1, self._b1, self.w2, self._b2, self.w3, self._b3,
-                   self.norm)
+                   self.norm, self.gate)
+
+    def set_gate(self, X, iters, excess=0.1):
+        """Gate on feature 3, log(|dt| sqrt(m/r^3)): the lowest value above
+        which the plain guess averages more than 2 + excess updates."""
+        f = np.asarray(X)[:, 3]
+        it = np.asarray(iters, np.float64)
+        edges = np.quantile(f, np.linspace(0, 1, 41))
+        gate = float("inf")
+        for a, b in zip(edges[:-1][::-1], edges[1:][::-1]):
+            sel = (f >= a) & (f <= b)
+            if sel.any() and it[sel].mean() > 2.0 + excess:
+                gate = float(a)
+            else:
+                break
+        self.gate = gate
+        return gate
 
     def save(self, path=WEIGHTS):
         np.savez(path, params=self.params.cpu().numpy(),
-                 norm=self.norm.cpu().numpy())
+                 norm=self.norm.cpu().numpy(), gate=np.float64(self.gate))
 
     @classmethod
     def load(cls, path=WEIGHTS):
@@ -195,16 +212,17 @@ class LearnedStart(object):
         z = np.load(path)
         obj.params.copy_(obj.torch.from_numpy(z["params"]))
         obj.norm.copy_(obj.torch.from_numpy(z["norm"]))
+        obj.gate = float(z["gate"]) if "gate" in z.files else float("-inf")
         obj._round()
         return obj
 
 
 def training_set(dts=(1.0 / 512,), seeds=range(1, 9), n_bodies=4096,
                  flags=(-1, 1)):
-    """(X, Y, states, m, e2, dt) of Kepler-branch pairs solved by the plain
-    solver on the GPU; Y = log(root / plain guess)."""
+    """(X, Y, iterations) of Kepler-branch pairs solved by the plain solver
+    on the GPU; Y = log(root / plain guess)."""
     import torch
-    Xs, Ys = [], []
+    Xs, Ys, Is = [], [], []
     for dt in dts:
         for seed in seeds:
             for flag in flags:
@@ -214,11 +232,13 @@ def training_set(dts=(1.0 / 512,), seeds=range(1, 9), n_bodies=4096,
                 out = torch.zeros((n, 6), dtype=torch.float64, device="cuda")
                 rx = torch.zeros((n, 4), dtype=torch.float32, device="cuda")
                 ry = torch.zeros(n, dtype=torch.float32, device="cuda")
-                kp.kepler_pairs(n, dt, T(m), T(e2), T(st), out, rec_x=rx,
-                                rec_y=ry)
+                it = torch.zeros(n, dtype=torch.int32, device="cuda")
+                kp.kepler_pairs(n, dt, T(m), T(e2), T(st), out, iters=it,
+                                rec_x=rx, rec_y=ry)
                 Xs.append(rx.cpu().numpy())
                 Ys.append(ry.cpu().numpy())
-    return np.concatenate(Xs), np.concatenate(Ys)
+                Is.append(it.cpu().numpy())
+    return np.concatenate(Xs), np.concatenate(Ys), np.concatenate(Is)
 
 
 def evaluate(net, dt, seeds=(101,), n_bodies=4096):
@@ -267,18 +287,20 @@ def main(argv=None):
     a = ap.parse_args(argv)
     dts = [float(x) for x in a.dts.split(",")]
     t0 = time.time()
-    X, Y = training_set(dts=dts, seeds=range(1, a.seeds + 1))
+    X, Y, I = training_set(dts=dts, seeds=range(1, a.seeds + 1))
     ok = np.isfinite(Y)
     t1 = time.time()
     net = LearnedStart(seed=0)
     hist = net.fit(X[ok], Y[ok], epochs=a.epochs)
     t2 = time.time()
+    net.set_gate(X[ok], I[ok])
     net.save(a.out)
     net.install()
     evals = [evaluate(net, dt) for dt in dts]
     kp.clear_mlp()
     print(json.dumps({"samples": int(ok.sum()), "data_s": t1 - t0,
-                      "train_s": t2 - t1, "loss": hist, "eval": evals}))
+                      "train_s": t2 - t1, "gate": net.gate, "loss": hist,
+                      "eval": evals}))
 
 
 if __name__ == "__main__":
