@@ -253,7 +253,7 @@ def test_split_phi_tstep_snap_accuracy():
         np.median(es), np.median(ec))
 
 
-@pytest.mark.parametrize("variant", range(7))
+@pytest.mark.parametrize("variant", range(9))
 @pytest.mark.parametrize("gsplit", [1, 3, 8])
 def test_split_every_variant(variant, gsplit):
     ps = ics.plummer(3000, eps=1e-4, seed=5)

@@ -51,7 +51,10 @@ def tune(kernel, ni, nj, reps=3, gsplits=GSPLITS, record=True):
             for g in gsplits:
                 if g > 1 and (nj + 255) // 256 < g:
                     continue
-                lib.set_split_config(kernel, v, g)
+                try:
+                    lib.set_split_config(kernel, v, g)
+                except lib.TupanGB300Error:
+                    break          # variant not compiled for this kernel
                 with torch.cuda.stream(stream):
                     lib.dev_sweep(kernel, ni, ip, nj, ip, op, scal=scal,
                                   mode=lib.MODE_SPLIT,
