@@ -146,6 +146,63 @@ def cpu_baseline(n, ni, ps):
                       "sphere (%.1f s)" % (ni, n, n, dt)}
 
 
+def kepler_solves(torch, stream):
+    """Second half of the metric: universal-Kepler pair solves per second on
+    the Kepler-branch pairs of a Sakura sweep (Salpeter Plummer N = 4096,
+    eps = 0, dt = 1/512: the config-5 half step), plain first guess and
+    learned start, and the queued Sakura sweep's pair rate."""
+    import numpy as np
+    from tupan_gb300 import ics, learned
+    from tupan_gb300 import kepler as kp
+    dt = 1.0 / 512
+    st, m, e2 = learned.kepler_pair_states(4096, 11, dt, flag=-1)
+    n = len(m)
+    T = lambda a: torch.from_numpy(np.ascontiguousarray(a)).cuda()
+    sm, se, ss = T(m), T(e2), T(st)
+    out = torch.zeros((n, 6), dtype=torch.float64, device="cuda")
+    it = torch.zeros(n, dtype=torch.int32, device="cuda")
+
+    def best(fn, reps=5):
+        fn()
+        torch.cuda.synchronize()
+        ts = []
+        for _ in range(reps):
+            a = torch.cuda.Event(enable_timing=True)
+            b = torch.cuda.Event(enable_timing=True)
+            a.record()
+            fn()
+            b.record()
+            torch.cuda.synchronize()
+            ts.append(a.elapsed_time(b) / 1e3)
+        return min(ts)
+
+    res = {"pairs": n, "dt": dt}
+    t = best(lambda: kp.kepler_pairs(n, dt, sm, se, ss, out, iters=it))
+    res["solves_per_s_plain"] = n / t
+    res["mean_iters_plain"] = float(it.float().mean().item())
+    try:
+        net = learned.LearnedStart.load()
+        net.install()
+        t = best(lambda: kp.kepler_pairs(n, dt, sm, se, ss, out, iters=it,
+                                         use_mlp=True))
+        res["solves_per_s_learned"] = n / t
+        res["mean_iters_learned"] = float(it.float().mean().item())
+        res["learned_gate"] = net.gate
+        kp.clear_mlp()
+    except (OSError, KeyError):
+        res["solves_per_s_learned"] = None
+    ps = ics.plummer(4096, eps=0.0, seed=11, masses="salpeter")
+    names = ("m", "rx", "ry", "rz", "e2", "vx", "vy", "vz")
+    d = {k: T(ps[k]) for k in names}
+    p = [d[k].data_ptr() for k in names]
+    o = [torch.zeros(4096, dtype=torch.float64, device="cuda")
+         for _ in range(6)]
+    op = [x.data_ptr() for x in o]
+    t = best(lambda: kp.sakura_queue(4096, p, 4096, p, op, dt, -1))
+    res["sakura_pairs_per_s"] = 4096 * 4096 / t
+    return res
+
+
 def run_reference(args):
     """--impl reference: the reference kernels' CPU path (the oracle port,
     bit-identical to tupan's C backend) on all host threads."""
@@ -334,6 +391,8 @@ def main():
     d2h = 8 * n * (3 + 6)
     e2e_val = world * inter / t_e2e / 1e9
 
+    kepler = kepler_solves(torch, stream) if rank == 0 else None
+
     if rank != 0:
         if world > 1:
             dist.destroy_process_group()
@@ -374,6 +433,7 @@ def main():
                 "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
                 "path": "acc_kernel + acc_jerk_kernel C-ABI, pinned host "
                         "arrays, SPLIT mode", "ms_per_step": t_e2e * 1e3},
+        "kepler": kepler,
         "gpu_launches": int(launches),
         "clocks": clk,
         "wall_s_timed": t_wall,
