@@ -118,6 +118,23 @@ class ClockSampler(object):
                 "reasons": sorted(reasons), "samples": len(sm)}
 
 
+def slowest_rank(times, world, device=None):
+    """Max over ranks of each per-step time (replicas: the job finishes with
+    its slowest rank).  Works on any process group backend (nccl, gloo)."""
+    if world <= 1:
+        return list(times)
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor(list(times), dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return t.tolist()
+
+
+def job_rate(interactions_per_rank, world, t_step):
+    """Whole-job Gint/s: every rank sweeps its own replica."""
+    return world * interactions_per_rank / t_step / 1e9
+
+
 def roofline_traffic():
     """dram bytes per AccJerk launch from the committed ncu summary."""
     path = os.path.join(ROOT, "profiles", "acc_jerk_split_n262144.md")
@@ -309,14 +326,10 @@ def main():
     launches = lib.load().tupan_gb300_launch_count() - launches0
     t_acc = sum(e[0].elapsed_time(e[1]) for e in ev) / 1e3 / args.steps
     t_aj = sum(e[1].elapsed_time(e[2]) for e in ev) / 1e3 / args.steps
-    t_step = t_acc + t_aj
-    if world > 1:
-        tt = torch.tensor([t_step, t_acc, t_aj], dtype=torch.float64,
-                          device=dev)
-        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
-        t_step, t_acc, t_aj = tt.tolist()
+    t_step, t_acc, t_aj = slowest_rank([t_acc + t_aj, t_acc, t_aj], world,
+                                       dev)
     inter = 2.0 * n * n
-    value = world * inter / t_step / 1e9
+    value = job_rate(inter, world, t_step)
 
     # accuracy of this run's AccJerk against the oracle on an i-subset
     acc_err = None
