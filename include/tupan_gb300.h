@@ -265,6 +265,135 @@ int tupan_gb300_acc_jerk_split_noalloc(
     const double *jvz, double *iax, double *iay, double *iaz, double *ijx,
     double *ijy, double *ijz, void *stream, unsigned *err_out);
 
+/* ------------------------------------------------------------------------
+ * Block time steps (libtupan_gb300.so only).  No counterpart in the
+ * reference, whose Hermite integrator (tupan/integrator/hermite.py:286-410)
+ * moves every particle with one shared step.  Each particle keeps a
+ * power-of-two step (the quantisation of tupan/integrator/__init__.py:59-78
+ * applied per particle, capped at dt_max); a block step predicts all
+ * particles to the next block time, sweeps forces for the active set only
+ * (compacted on the device) and corrects those particles with epec(2).
+ * ---------------------------------------------------------------------- */
+/* Host arrays are copied in; forces and steps are initialised at t = 0.
+ * order 4, 6 or 8; mode 0 EXACT, 1 SPLIT. */
+int tupan_gb300_block_create(uint64_t n, int order, int mode, double eta,
+                             double dt_max, const double *m, const double *e2,
+                             const double *rx, const double *ry,
+                             const double *rz, const double *vx,
+                             const double *vy, const double *vz,
+                             void **handle);
+/* Block steps until t >= t_end or max_steps (0: no limit); returns the time
+ * reached, the steps taken and the sum of active-set sizes over them. */
+int tupan_gb300_block_evolve(void *handle, double t_end, long long max_steps,
+                             double *t_out, long long *steps_out,
+                             long long *active_out);
+/* Positions and velocities at each particle's own last time t[i], and its
+ * current step dt[i] (host arrays of n). */
+int tupan_gb300_block_get_state(void *handle, double *rx, double *ry,
+                                double *rz, double *vx, double *vy,
+                                double *vz, double *t, double *dt);
+int tupan_gb300_block_destroy(void *handle);
+
+/* ------------------------------------------------------------------------
+ * Sakura and Kepler (libtupan_gb300.so only).  The pair arithmetic is that
+ * of sakura_kernel (libtupan.h:203-229) and kepler_solver_kernel
+ * (libtupan.h:231-246); these entry points reorganise its schedule: the
+ * pairs that need the universal Kepler solver are queued and solved by a
+ * separate pass, so one expensive pair does not stall a warp of cheap
+ * ones.  All pointers are DEVICE pointers unless marked host.  Status 3:
+ * a solve used up the retry budget (0: 2^20 single-step solves).
+ * ---------------------------------------------------------------------- */
+/* Learned start of the universal-anomaly iteration: bf16 weights w1 (64x4),
+ * w2 (64x64), w3 (64), fp32 biases b1 b2 b3 and norm[8] = mean[4],
+ * 1/std[4] of the features.  The network replaces the plain starting guess
+ * only where the feature log(|dt| sqrt(m/r^3)) exceeds gate.  w1 == NULL
+ * removes it.  The arrays must outlive the installation. */
+int tupan_gb300_kepler_set_mlp(const void *w1, const float *b1,
+                               const void *w2, const float *b2,
+                               const void *w3, const float *b3,
+                               const float *norm, float gate);
+/* n independent pairs over dt: m[n], e2[n], state[n x 6] (relative r, v)
+ * -> out[n x 6].  iters[n] (Laguerre updates), rec_x[n x 4] and rec_y[n]
+ * (learned-start features and targets) may be NULL.  Synchronous. */
+int tupan_gb300_kepler_pairs(uint64_t n, double dt, const double *m,
+                             const double *e2, const double *state,
+                             double *out, int *iters, float *rec_x,
+                             float *rec_y, int use_mlp, long long budget,
+                             void *stream);
+/* sakura_kernel on device arrays: i_attrs / j_attrs are 8 pointers each in
+ * the kernel's order (m, rx, ry, rz, e2, vx, vy, vz), outs 6 (drx .. dvz);
+ * flag -1 or +1.  *n_kepler (host) receives the number of queued pairs;
+ * kepler_iters (host, 65 bins, may be NULL) accumulates their update
+ * counts.  Synchronous. */
+int tupan_gb300_sakura_queue(uint64_t ni, const void *const *i_attrs,
+                             uint64_t nj, const void *const *j_attrs,
+                             double dt, int64_t flag, void *const *outs,
+                             int use_mlp, long long budget, void *stream,
+                             unsigned long long *n_kepler,
+                             long long *kepler_iters);
+/* Device-resident Sakura integrator (tupan/integrator/sakura.py:100-117,
+ * fixed step): drift tau/2, two queued Sakura half-sweeps, drift tau/2. */
+int tupan_gb300_sakura_create(uint64_t n, const double *m, const double *e2,
+                              const double *rx, const double *ry,
+                              const double *rz, const double *vx,
+                              const double *vy, const double *vz,
+                              void **handle);
+int tupan_gb300_sakura_evolve(void *handle, double tau, double t_end,
+                              int use_mlp, double *t_out,
+                              long long *steps_out, long long *kepler_out,
+                              long long *kepler_iters);
+int tupan_gb300_sakura_get_state(void *handle, double *rx, double *ry,
+                                 double *rz, double *vx, double *vy,
+                                 double *vz);
+int tupan_gb300_sakura_destroy(void *handle);
+
+/* ------------------------------------------------------------------------
+ * Training kernels of the learned Kepler start (4 -> 64 -> 64 -> 1, SiLU),
+ * libtupan_gb300.so only; no counterpart in the reference.  The parameter
+ * vector is fp32 (tupan_gb300_mlp_param_count entries); the forward pass
+ * uses bf16 weights with fp32 accumulation.  Device pointers throughout.
+ * ---------------------------------------------------------------------- */
+int tupan_gb300_mlp_param_count(void);
+/* bf16 copies w1 w2 w3 of params' weights and rw = params with its weights
+ * rounded through bf16 (what the forward pass computes with). */
+int tupan_gb300_mlp_round(const float *params, void *w1, void *w2, void *w3,
+                          float *rw, void *stream);
+/* grad += d/dparams of scale * sum (net(X) - Y)^2 over n samples
+ * (X: n x 4 raw features); *loss += the sum of squared errors. */
+int tupan_gb300_mlp_grad(const float *rw, const float *norm, const float *X,
+                         const float *Y, uint64_t n, float scale,
+                         float *grad, float *loss, void *stream);
+/* One Adam step (beta 0.9 / 0.999, eps 1e-8) at step >= 1; zeroes grad. */
+int tupan_gb300_mlp_adam(float *params, float *m, float *v, float *grad,
+                         float lr, int step, void *stream);
+
+/* ------------------------------------------------------------------------
+ * Ensembles (libtupan_gb300.so only; no counterpart in the reference, which
+ * integrates one system per process).  n_sys independent systems of 1..512
+ * particles each, concatenated in host arrays with offsets sys_off[n_sys +
+ * 1]; every system takes its own shared adaptive Hermite-4 steps
+ * (SPLIT forces), all systems advancing in one persistent sweep per force
+ * evaluation.
+ * ---------------------------------------------------------------------- */
+int tupan_gb300_ensemble_create(unsigned n_sys, const uint64_t *sys_off,
+                                double eta, const double *m, const double *e2,
+                                const double *rx, const double *ry,
+                                const double *rz, const double *vx,
+                                const double *vy, const double *vz,
+                                void **handle);
+/* Steps every system to t_end, `batch` steps per graph replay; *max_steps_out
+ * (host) receives the largest step count over systems. */
+int tupan_gb300_ensemble_evolve(void *handle, double t_end, int batch,
+                                long long *max_steps_out);
+/* Per-system kinetic and potential energies (host arrays of n_sys). */
+int tupan_gb300_ensemble_energy(void *handle, double *ke, double *pe);
+/* Per-system time and step count (host, n_sys) and the concatenated state
+ * (host, n). */
+int tupan_gb300_ensemble_get(void *handle, double *t, long long *nsteps,
+                             double *rx, double *ry, double *rz, double *vx,
+                             double *vy, double *vz);
+int tupan_gb300_ensemble_destroy(void *handle);
+
 #ifdef __cplusplus
 }
 #endif

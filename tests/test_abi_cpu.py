@@ -33,12 +33,31 @@ def built():
 
 
 def float64_only():
-    """Header functions the float32 library does not export: everything
-    after the first 'libtupan_gb300.so only' / 'No counterpart' section that
-    works on double data only (device drivers and the no-alloc sweep)."""
+    """Header functions the float32 library does not export: the sections
+    marked 'libtupan_gb300.so only' (device drivers, Sakura/Kepler queue,
+    learned-start training, ensembles) and the no-alloc sweep."""
+    prefixes = ("tupan_gb300_hermite_", "tupan_gb300_block_",
+                "tupan_gb300_sakura_", "tupan_gb300_kepler_",
+                "tupan_gb300_mlp_", "tupan_gb300_ensemble_")
     return {n for n in header_functions()
-            if n.startswith("tupan_gb300_hermite_")
-            or n.endswith("_noalloc")}
+            if n.startswith(prefixes) or n.endswith("_noalloc")}
+
+
+def test_float64_library_exports_nothing_undeclared(built):
+    """Every tupan_gb300_* function the float64 library exports is declared
+    in the header."""
+    import subprocess
+    path = lib.library_path("float64")
+    try:
+        out = subprocess.run(["nm", "-D", "--defined-only", path],
+                             capture_output=True, text=True, check=True).stdout
+    except (OSError, subprocess.CalledProcessError):
+        pytest.skip("nm not available")
+    exported = {ln.split()[-1] for ln in out.splitlines()
+                if len(ln.split()) == 3 and ln.split()[1] == "T"}
+    ours = {n for n in exported if n.startswith("tupan_gb300_")}
+    extra = sorted(ours - set(header_functions()))
+    assert not extra, extra
 
 
 @pytest.mark.parametrize("prec", ["float64", "float32"])
