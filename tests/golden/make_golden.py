@@ -271,10 +271,73 @@ def integrators(refroot):
     print("wrote", fn, os.path.getsize(fn))
 
 
+SIA_RUNS = [
+    # (method, n, eps, masses, eta, t_end, max_steps, seed)
+    ("sia21h.dkd", 48, 1e-4, "salpeter", 1.0 / 32, 0.25, 6, 31),
+    ("sia21h.kdk", 48, 1e-4, "salpeter", 1.0 / 32, 0.25, 6, 32),
+    ("sia21a.dkd", 40, 1e-4, "equal", 1.0 / 32, 0.25, 8, 33),
+    ("sia21s.kdk", 40, 1e-4, "equal", 1.0 / 64, 0.25, 8, 34),
+    ("sia22h.dkd", 40, 1e-4, "salpeter", 1.0 / 32, 0.25, 4, 35),
+    ("sia43h.kdk", 32, 1e-4, "salpeter", 1.0 / 32, 0.25, 2, 36),
+    ("sia44a.dkd", 40, 1e-4, "salpeter", 1.0 / 32, 0.25, 4, 37),
+    ("sia45s.dkd", 32, 1e-4, "equal", 1.0 / 64, 0.25, 4, 38),
+    ("sia46h.kdk", 32, 1e-4, "salpeter", 1.0 / 32, 0.25, 2, 39),
+    ("sia67a.kdk", 32, 1e-4, "equal", 1.0 / 32, 0.25, 3, 40),
+    ("sia69h.dkd", 16, 1e-4, "equal", 1.0 / 32, 0.25, 1, 41),
+    ("sia21h.dkd", 3, 0.0, "salpeter", 1.0 / 16, 0.25, 6, 42),
+]
+
+
+def sia(refroot):
+    """Short runs of the reference's SIA integrators (tupan/integrator/
+    sia.py:965-1123) on its C backend.  SIA reorders the particle system at
+    every split/join, so the final state is stored in the reference's final
+    order together with each particle's id, time, nstep and tstep."""
+    sys.path.insert(0, refroot)
+    sys.path.insert(0, os.path.dirname(os.path.dirname(HERE)))
+    from tupan.integrator import Integrator
+    from tupan.particles.allparticles import ParticleSystem
+    from tupan_gb300 import ics
+
+    store = {}
+    for r, (method, n, eps, masses, eta, t_end, max_steps, seed) in \
+            enumerate(SIA_RUNS):
+        d = ics.plummer(n, eps=eps, seed=seed, masses=masses)
+        ps = ParticleSystem(n)
+        ps.id[...] = np.arange(n)
+        ps.mass[...] = d["m"]
+        ps.eps2[...] = d["e2"]
+        for k in ("rx", "ry", "rz", "vx", "vy", "vz"):
+            getattr(ps, k)[...] = d[k]
+        tag = "%d/" % r
+        store[tag + "method"] = np.array(method)
+        for k in ("m", "e2", "rx", "ry", "rz", "vx", "vy", "vz"):
+            store[tag + "in/" + k] = d[k].copy()
+        integ = Integrator(eta, 0.0, ps, method=method)
+        times = []
+        while abs(integ.time) < t_end and len(times) < max_steps:
+            integ.evolve_step(t_end)
+            times.append(integ.time)
+        ps = integ.particle_system
+        store[tag + "times"] = np.array(times)
+        store[tag + "params"] = np.array([eta, t_end, max_steps])
+        for k in ("id", "rx", "ry", "rz", "vx", "vy", "vz", "time", "nstep",
+                  "tstep"):
+            store[tag + "out/" + k] = np.array(getattr(ps, k), copy=True)
+        print(method, n, len(times), "steps, t =", integ.time,
+              "nstep range", int(ps.nstep.min()), int(ps.nstep.max()))
+    fn = os.path.join(HERE, "golden_sia.npz")
+    np.savez_compressed(fn, **store)
+    print("wrote", fn, os.path.getsize(fn))
+
+
 if __name__ == "__main__":
     ref = sys.argv[1] if len(sys.argv) > 1 else "/root/reference"
     if "--integrators" in sys.argv:
         integrators(ref)
+    elif "--sia" in sys.argv:
+        sia(ref)
     else:
         main(ref)
         integrators(ref)
+        sia(ref)
