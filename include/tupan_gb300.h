@@ -394,6 +394,38 @@ int tupan_gb300_ensemble_get(void *handle, double *t, long long *nsteps,
                              double *vy, double *vz);
 int tupan_gb300_ensemble_destroy(void *handle);
 
+/* ------------------------------------------------------------------------
+ * SIA integrators (libtupan_gb300.so only).  No counterpart in the
+ * reference's C ABI: tupan/integrator/sia.py:965-1123 runs the recursion on
+ * host arrays, copying the particle system at every split.  Here the system
+ * stays in HBM, a split is a stable in-place partition of an index range,
+ * and every force sweep runs on sub-ranges; with mode 0 (EXACT) a run is
+ * bit-identical to the reference's except where a two-body subsystem calls
+ * the Kepler solver.  Newtonian only.
+ * ---------------------------------------------------------------------- */
+/* method: "sia21s.dkd" .. "sia69h.kdk"; mode 0 EXACT, 1 SPLIT sweeps. */
+int tupan_gb300_sia_create(uint64_t n, const char *method, double eta,
+                           int mode, const double *m, const double *e2,
+                           const double *rx, const double *ry,
+                           const double *rz, const double *vx,
+                           const double *vy, const double *vz,
+                           void **handle);
+/* Base steps until |t| >= t_end or max_steps (0: no limit); t_log (host,
+ * may be NULL) receives the time after each step (at most log_cap).
+ * Status 5: recursion deeper than 512 levels. */
+int tupan_gb300_sia_evolve(void *handle, double t_end, long long max_steps,
+                           double *t_out, long long *steps_out,
+                           double *t_log, long long log_cap);
+/* Current particle order (the reference's order after its joins). */
+int tupan_gb300_sia_get_state(void *handle, long long *id, double *rx,
+                              double *ry, double *rz, double *vx, double *vy,
+                              double *vz, double *time, long long *nstep,
+                              double *tstep);
+/* stats[6]: recursion calls, Kepler solves, sweeps, partitions, deepest
+ * level, base steps. */
+int tupan_gb300_sia_stats(void *handle, long long *stats);
+int tupan_gb300_sia_destroy(void *handle);
+
 #ifdef __cplusplus
 }
 #endif

@@ -38,7 +38,8 @@ def float64_only():
     learned-start training, ensembles) and the no-alloc sweep."""
     prefixes = ("tupan_gb300_hermite_", "tupan_gb300_block_",
                 "tupan_gb300_sakura_", "tupan_gb300_kepler_",
-                "tupan_gb300_mlp_", "tupan_gb300_ensemble_")
+                "tupan_gb300_mlp_", "tupan_gb300_ensemble_",
+                "tupan_gb300_sia_")
     return {n for n in header_functions()
             if n.startswith(prefixes) or n.endswith("_noalloc")}
 

@@ -37,11 +37,12 @@ UNITS = {
     "mlp.o": ("mlp.cu", []),
     "ensemble.o": ("ensemble.cu", ["-fmad=false"]),
     "noalloc.o": ("noalloc.cu", []),
+    "sia.o": ("sia.cu", ["-fmad=false"]),
 }
 LINKS = {
     LIB64: ["exact.o", "split.o", "abi64.o", "microbench.o", "driver.o",
             "blockstep.o", "sakura.o", "mlp.o", "ensemble.o",
-            "noalloc.o"],
+            "noalloc.o", "sia.o"],
     LIB32: ["exact.o", "split.o", "abi32.o", "microbench.o"],
 }
 

@@ -184,3 +184,101 @@ class DeviceBlockHermite(object):
             self.close()
         except Exception:
             pass
+
+
+def _declare_sia(L):
+    c = ctypes
+    lp = c.POINTER(c.c_longlong)
+    L.tupan_gb300_sia_create.argtypes = (
+        [c.c_uint64, c.c_char_p, c.c_double, c.c_int] + [_DP] * 8
+        + [c.POINTER(c.c_void_p)])
+    L.tupan_gb300_sia_create.restype = c.c_int
+    L.tupan_gb300_sia_evolve.argtypes = [c.c_void_p, c.c_double, c.c_longlong,
+                                         _DP, lp, _DP, c.c_longlong]
+    L.tupan_gb300_sia_evolve.restype = c.c_int
+    L.tupan_gb300_sia_get_state.argtypes = ([c.c_void_p, lp] + [_DP] * 7
+                                            + [lp, _DP])
+    L.tupan_gb300_sia_get_state.restype = c.c_int
+    L.tupan_gb300_sia_stats.argtypes = [c.c_void_p, lp]
+    L.tupan_gb300_sia_stats.restype = c.c_int
+    L.tupan_gb300_sia_destroy.argtypes = [c.c_void_p]
+    L.tupan_gb300_sia_destroy.restype = c.c_int
+
+
+SIA_METHODS = tuple("sia%s%s.%s" % (s, m, k)
+                    for s in ("21", "22", "43", "44", "45", "46", "67", "69")
+                    for m in "sah" for k in ("dkd", "kdk"))
+
+
+class DeviceSIA(object):
+    """tupan's SIA integrators (tupan/integrator/sia.py; methods
+    ``sia21s.dkd`` .. ``sia69h.kdk``) with the particles in HBM; see
+    csrc/sia.cu.  The particle order changes at every split like the
+    reference's; ``state()`` returns it with each particle's ``id``.
+    Newtonian only."""
+
+    def __init__(self, ps, method, eta, mode="exact"):
+        if method not in SIA_METHODS:
+            raise ValueError("unexpected SIA method: %r" % (method,))
+        self.L = lib.load("float64")
+        _declare_sia(self.L)
+        self.n = len(ps["m"])
+        arrs = [np.ascontiguousarray(ps[k], dtype=np.float64)
+                for k in ("m", "e2", "rx", "ry", "rz", "vx", "vy", "vz")]
+        h = ctypes.c_void_p()
+        st = self.L.tupan_gb300_sia_create(
+            self.n, method.encode(), float(eta),
+            lib.MODE_SPLIT if mode == "split" else lib.MODE_EXACT,
+            *[_p(a) for a in arrs], ctypes.byref(h))
+        if st:
+            raise lib.TupanGB300Error("sia_create failed: status %d" % st)
+        self.h = h
+        self.time = 0.0
+
+    def evolve(self, t_end, max_steps=0):
+        """Base steps until |t| >= t_end (or max_steps); returns the time
+        after each step taken by this call."""
+        cap = int(max_steps) if max_steps else 1 << 16
+        log = np.zeros(cap)
+        t = ctypes.c_double()
+        k = ctypes.c_longlong()
+        st = self.L.tupan_gb300_sia_evolve(self.h, float(t_end),
+                                           int(max_steps), ctypes.byref(t),
+                                           ctypes.byref(k), _p(log), cap)
+        if st:
+            raise lib.TupanGB300Error("sia_evolve failed: status %d" % st)
+        self.time = t.value
+        return log[:min(k.value, cap)].copy()
+
+    def state(self):
+        out = {k: np.empty(self.n) for k in
+               ("rx", "ry", "rz", "vx", "vy", "vz", "time", "tstep")}
+        out["id"] = np.empty(self.n, dtype=np.int64)
+        out["nstep"] = np.empty(self.n, dtype=np.int64)
+        lp = ctypes.POINTER(ctypes.c_longlong)
+        st = self.L.tupan_gb300_sia_get_state(
+            self.h, out["id"].ctypes.data_as(lp),
+            *[_p(out[k]) for k in ("rx", "ry", "rz", "vx", "vy", "vz",
+                                   "time")],
+            out["nstep"].ctypes.data_as(lp), _p(out["tstep"]))
+        if st:
+            raise lib.TupanGB300Error("sia_get_state failed")
+        return out
+
+    def stats(self):
+        s = np.zeros(6, dtype=np.int64)
+        self.L.tupan_gb300_sia_stats(
+            self.h, s.ctypes.data_as(ctypes.POINTER(ctypes.c_longlong)))
+        return dict(zip(("recursions", "kepler", "sweeps", "partitions",
+                         "max_depth", "steps"), (int(x) for x in s)))
+
+    def close(self):
+        if self.h:
+            self.L.tupan_gb300_sia_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
