@@ -421,9 +421,16 @@ int tupan_gb300_sia_get_state(void *handle, long long *id, double *rx,
                               double *ry, double *rz, double *vx, double *vy,
                               double *vz, double *time, long long *nstep,
                               double *tstep);
-/* stats[6]: recursion calls, Kepler solves, sweeps, partitions, deepest
- * level, base steps. */
+/* stats[9]: recursion calls, Kepler solves, host-launched sweeps,
+ * partitions, deepest level, base steps, single-CTA subtree launches, the
+ * microseconds spent in them, and the pair interactions summed (ni * nj of
+ * every Acc and Tstep sum). */
 int tupan_gb300_sia_stats(void *handle, long long *stats);
+/* Subsystems of at most max_n (0 .. 128) particles run the rest of their
+ * recursion inside one CTA, staged in shared memory; 0 drives every level
+ * from the host.  Both paths give the same bits.  Returns the previous
+ * value, or -1 for a bad argument. */
+int tupan_gb300_sia_set_subtree(void *handle, int max_n);
 int tupan_gb300_sia_destroy(void *handle);
 
 #ifdef __cplusplus

@@ -34,10 +34,12 @@ def load(r):
             int(max_steps), z[tag + "times"], out)
 
 
+@pytest.mark.parametrize("subtree", [0, 16, 128])
 @pytest.mark.parametrize("r", runs())
-def test_exact_sia_matches_reference(r):
+def test_exact_sia_matches_reference(r, subtree):
     method, ps, eta, t_end, max_steps, times, out = load(r)
     d = DeviceSIA(ps, method, eta, mode="exact")
+    d.set_subtree(subtree)
     got = d.evolve(t_end, max_steps=max_steps)
     st = d.state()
     kep = d.stats()["kepler"]
@@ -73,6 +75,41 @@ def test_exact_sia_matches_oracle_at_larger_n(method):
             np.testing.assert_array_equal(st[k], ref[k], err_msg=k)
         else:
             assert np.abs(st[k] - ref[k]).max() <= 1e-9 * np.abs(ref[k]).max()
+
+
+@pytest.mark.parametrize("method", ["sia21h.dkd", "sia43h.kdk", "sia45a.dkd"])
+def test_subtree_and_host_paths_give_identical_bits(method):
+    ps = ics.plummer(600, eps=1e-3, seed=12, masses="salpeter")
+    res = []
+    for sub in (0, 128):
+        d = DeviceSIA(ps, method, 1.0 / 64, mode="exact")
+        d.set_subtree(sub)
+        d.evolve(1.0, max_steps=2)
+        res.append((d.state(), d.stats()))
+        d.close()
+    (a, sa), (b, sb) = res
+    for k in ("id", "nstep") + STATE:
+        np.testing.assert_array_equal(a[k], b[k], err_msg=k)
+    assert sa["recursions"] == sb["recursions"]
+    assert sa["kepler"] == sb["kepler"]
+    assert sa["max_depth"] == sb["max_depth"]
+
+
+def test_split_subtree_close_to_host_path():
+    # SPLIT sums in the single-CTA kernel (FP32 runs added in double) and in
+    # the sweep kernels (Kahan-folded lanes) differ only by rounding.
+    ps = ics.plummer(100, eps=1e-3, seed=21)
+    res = []
+    for sub in (0, 128):
+        d = DeviceSIA(ps, "sia44s.kdk", 1.0 / 128, mode="split")
+        d.set_subtree(sub)
+        d.evolve(1.0, max_steps=3)
+        res.append(d.state())
+        d.close()
+    a, b = res
+    np.testing.assert_array_equal(a["id"], b["id"])
+    for k, tol in (("rx", 1e-10), ("vx", 1e-8), ("vz", 1e-8)):
+        assert np.abs(a[k] - b[k]).max() <= tol * np.abs(a[k]).max(), k
 
 
 def test_split_sia_shared_steps_close_to_exact():

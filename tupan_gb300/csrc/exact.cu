@@ -113,19 +113,12 @@ __global__ void exact_kepler(const Sweep s, long long budget, unsigned *err)
         b[k] = ((const R *)s.ip[k])[1];
     }
     const R dt = R(s.scal[0]);
-    R p0[6], p1[6], m, e2;
-    pair_state(a, b, p0, &m, &e2);
-    R amu = a[0] / m;
-    R bmu = b[0] / m;
-    R cm[6];
-    for (int c = 0; c < 3; ++c) cm[c] = amu * a[1 + c] + bmu * b[1 + c];
-    for (int c = 0; c < 3; ++c) cm[3 + c] = amu * a[5 + c] + bmu * b[5 + c];
-    for (int c = 0; c < 3; ++c) cm[c] += cm[3 + c] * dt;
     KepCtx<R> ctx = {0, budget, 0, false, false, R(0)};
-    kep_solve(dt, m, e2, p0, p1, ctx);
+    R a1[6], b1[6];
+    kepler_two_body(a, b, dt, a1, b1, ctx);
     for (int q = 0; q < 6; ++q) {
-        ((R *)s.out[q])[0] = cm[q] + bmu * p1[q];
-        ((R *)s.out[q])[1] = cm[q] - amu * p1[q];
+        ((R *)s.out[q])[0] = a1[q];
+        ((R *)s.out[q])[1] = b1[q];
     }
     if (ctx.exhausted) atomicOr(err, (unsigned)DERR_KEPLER_BUDGET);
 }

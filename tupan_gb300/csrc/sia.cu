@@ -10,7 +10,8 @@
 // every later pairwise sum -- is exactly the reference's.  The recursion
 // (SIA.recurse, sia.py:1097-1123) runs on the host, as in the reference; it
 // reads back one count per split (and the minimum step per level in shared-
-// adaptive mode).  Forces use the library's sweeps on sub-ranges: in EXACT
+// adaptive mode).  A subsystem of at most 128 particles is handed whole to
+// one CTA that runs the rest of its recursion on the device.  Forces use the library's sweeps on sub-ranges: in EXACT
 // mode every sweep is bit-identical to the reference C, and the drift,
 // kick and bookkeeping kernels are compiled with -fmad=false and round like
 // numpy, so a run matches the reference integrator bit for bit except where
@@ -26,10 +27,14 @@
 #include <string.h>
 
 #include <cfloat>
+#include <chrono>
 #include <utility>
 #include <vector>
 
 #include "tg_common.cuh"
+#include "tg_kepler.cuh"
+#include "tg_pairs.cuh"
+#include "tg_split_ops.cuh"
 
 #define TG_EXPORT extern "C" __attribute__((visibility("default")))
 
@@ -228,6 +233,405 @@ k_partition(Fields F, Fields S, uint64_t lo, uint64_t n, double thr,
 }
 
 // ---------------------------------------------------------------------------
+// Small subsystems: the whole recursion below one call of SIA.recurse in a
+// single CTA.  Deep in the hierarchy the subsystems hold a handful of
+// particles and the host-driven path would spend a launch and a host round
+// trip on every few-pair sweep; here the subsystem is staged in shared
+// memory, the recursion runs on an explicit stack, and every operation --
+// Tstep and Acc sums (one i per thread, j in order, the EXACT pair
+// arithmetic), block quantisation, stable partition, drift, kick, Kepler
+// for two-body subsystems -- is the same arithmetic as the sweeps the host
+// path launches, so both paths give identical bits.
+// ---------------------------------------------------------------------------
+constexpr int SUB_MAX = 128;       // particles (one per thread)
+constexpr int SUB_DEPTH = 64;      // recursion levels below the entry
+constexpr int SEQ_MAX = 19;        // longest propagator (sia69)
+
+struct SubParams {
+    int seq_len;
+    int outer[SEQ_MAX];
+    double coef[SEQ_MAX];
+    int mode;            // 's', 'a' or 'h'
+    int kdk;
+    int split;           // 1: SPLIT-mode sums (FP32 pairs, DS positions)
+    double eta;
+    long long budget;
+};
+
+// In/out block of one subtree launch.
+struct SubCtl {
+    double t_curr;
+    unsigned status;     // 0 ok, 1 recursion deeper than SUB_DEPTH
+    int max_depth;
+    long long n_recurse, n_kepler, n_partitions;
+    unsigned long long interactions;
+};
+
+struct Frame {
+    int lo, n, ns, step, sub;
+    double tau;
+};
+
+__device__ double d_block_tstep(double min_ts, double t, double tau)
+{
+    // tupan/integrator/__init__.py:59-78
+    long long power = (long long)(log2(min_ts) - 1.0);
+    double min_bts = ldexp(1.0, (int)power);
+    const double t_next = t + min_bts;
+    for (int k = 0; k < 2100 && fmod(t_next, min_bts) != 0.0; ++k)
+        min_bts /= 2.0;
+    min_bts = copysign(min_bts, tau);
+    if (fabs(min_bts) > fabs(tau)) min_bts = tau;
+    return min_bts;
+}
+
+struct SubState {
+    double f[NFIELD][SUB_MAX];
+    double x[NFIELD][SUB_MAX];     // partition scratch
+    float g[11][SUB_MAX];          // SPLIT images: xh yh zh m xl yl zl e2 v
+    Frame stk[SUB_DEPTH];
+    int sp;
+    double t_curr;
+    unsigned status;
+    int max_depth;
+    long long n_recurse, n_kepler, n_partitions;
+    unsigned long long interactions;
+    double red[SUB_MAX / 32];
+    unsigned wc[SUB_MAX / 32];
+    int ns;
+    double tau;
+};
+
+// i in [ilo, ilo + ni) against j in [jlo, jlo + nj): Acc (out: ax ay az) or
+// Tstep (out: tstep tstepij), thread t owns i = ilo + t.
+template <class Op>
+__device__ void sub_sweep(SubState &S, int ilo, int ni, int jlo, int nj,
+                          int first_out, const Sweep &sw)
+{
+    const int t = threadIdx.x;
+    if (t == 0) S.interactions += (unsigned long long)ni * nj;
+    if (t < ni) {
+        double ip[Op::NA], jp[Op::NA], o[Op::NO];
+#pragma unroll
+        for (int a = 0; a < Op::NA; ++a) ip[a] = S.f[a][ilo + t];
+        Op::init(o);
+        for (int j = 0; j < nj; ++j) {
+#pragma unroll
+            for (int a = 0; a < Op::NA; ++a) jp[a] = S.f[a][jlo + j];
+            Op::pair(ip, jp, o, sw);
+        }
+        Op::finish(ip, o, sw);
+#pragma unroll
+        for (int c = 0; c < Op::NO; ++c) S.f[first_out + c][ilo + t] = o[c];
+    }
+    __syncthreads();
+}
+
+// SPLIT mode: the same FP32 pair operators as the sweep kernels on
+// double-single images of the subsystem, each run of 16 pair terms summed
+// in FP32 and added to a double accumulator.
+__device__ void sub_images(SubState &S, int lo, int n)
+{
+    const int t = threadIdx.x;
+    if (t < n) {
+        const int i = lo + t;
+        split2(S.f[F_RX][i], S.g[0][i], S.g[4][i]);
+        split2(S.f[F_RY][i], S.g[1][i], S.g[5][i]);
+        split2(S.f[F_RZ][i], S.g[2][i], S.g[6][i]);
+        S.g[3][i] = (float)S.f[F_M][i];
+        S.g[7][i] = (float)S.f[F_E2][i];
+        S.g[8][i] = (float)S.f[F_VX][i];
+        S.g[9][i] = (float)S.f[F_VY][i];
+        S.g[10][i] = (float)S.f[F_VZ][i];
+    }
+}
+
+template <class Op>
+__device__ typename Op::P sub_image(const SubState &S, int i)
+{
+    typename AccJerkS::P p = {S.g[0][i], S.g[1][i], S.g[2][i], S.g[3][i],
+                              S.g[4][i], S.g[5][i], S.g[6][i], S.g[7][i],
+                              S.g[8][i], S.g[9][i], S.g[10][i]};
+    if constexpr (sizeof(typename Op::P) == sizeof(typename AccJerkS::P)) {
+        return p;
+    } else {
+        return {p.xh, p.yh, p.zh, p.m, p.xl, p.yl, p.zl, p.e2};
+    }
+}
+
+template <class Op>
+__device__ void sub_split_sweep(SubState &S, int ilo, int ni, int jlo, int nj,
+                                int first_out, double eta)
+{
+    sub_images(S, ilo, ni);
+    sub_images(S, jlo, nj);
+    __syncthreads();
+    const int t = threadIdx.x;
+    if (t == 0) S.interactions += (unsigned long long)ni * nj;
+    if (t < ni) {
+        const typename Op::P ip = sub_image<Op>(S, ilo + t);
+        double v[Op::NO];
+        float part[Op::NO];
+#pragma unroll
+        for (int c = 0; c < Op::NO; ++c) v[c] = 0.0;
+        for (int j0 = 0; j0 < nj; j0 += 16) {
+#pragma unroll
+            for (int c = 0; c < Op::NO; ++c) part[c] = 0.f;
+            const int je = j0 + 16 < nj ? j0 + 16 : nj;
+            for (int j = j0; j < je; ++j)
+                Op::pair(ip, sub_image<Op>(S, jlo + j), part, (float)eta);
+#pragma unroll
+            for (int c = 0; c < Op::NO; ++c)
+                v[c] = c == Op::MAXC ? fmax(v[c], (double)part[c])
+                                     : v[c] + (double)part[c];
+        }
+        Op::finish(v, eta);
+#pragma unroll
+        for (int c = 0; c < Op::NO; ++c) S.f[first_out + c][ilo + t] = v[c];
+    }
+    __syncthreads();
+}
+
+__device__ void sub_acc(SubState &S, int ilo, int ni, int jlo, int nj,
+                        const SubParams &P, const Sweep &acc)
+{
+    if (P.split) sub_split_sweep<AccS>(S, ilo, ni, jlo, nj, F_AX, 0.0);
+    else sub_sweep<AccPair<double>>(S, ilo, ni, jlo, nj, F_AX, acc);
+}
+
+__device__ void sub_drift(SubState &S, int lo, int n, double c)
+{
+    const int t = threadIdx.x;
+    if (t < n) {
+        const int i = lo + t;
+        S.f[F_RX][i] = S.f[F_RX][i] + S.f[F_VX][i] * c;
+        S.f[F_RY][i] = S.f[F_RY][i] + S.f[F_VY][i] * c;
+        S.f[F_RZ][i] = S.f[F_RZ][i] + S.f[F_VZ][i] * c;
+    }
+    __syncthreads();
+}
+
+__device__ void sub_kick(SubState &S, int lo, int n, double c)
+{
+    const int t = threadIdx.x;
+    if (t < n) {
+        const int i = lo + t;
+        S.f[F_VX][i] = S.f[F_VX][i] + S.f[F_AX][i] * c;
+        S.f[F_VY][i] = S.f[F_VY][i] + S.f[F_AY][i] * c;
+        S.f[F_VZ][i] = S.f[F_VZ][i] + S.f[F_AZ][i] * c;
+    }
+    __syncthreads();
+}
+
+__device__ void sub_fewbody(SubState &S, int lo, int n, double tau,
+                            const SubParams &P, unsigned *err)
+{
+    if (n == 1) {
+        sub_drift(S, lo, 1, tau);
+        return;
+    }
+    if (n == 2) {
+        if (threadIdx.x == 0) {
+            double a[8], b[8], a1[6], b1[6];
+            for (int k = 0; k < 8; ++k) {
+                a[k] = S.f[k][lo];
+                b[k] = S.f[k][lo + 1];
+            }
+            KepCtx<double> ctx = {0, P.budget, 0, false, false, 0.0};
+            kepler_two_body(a, b, tau, a1, b1, ctx);
+            const int outs[6] = {F_RX, F_RY, F_RZ, F_VX, F_VY, F_VZ};
+            for (int q = 0; q < 6; ++q) {
+                S.f[outs[q]][lo] = a1[q];
+                S.f[outs[q]][lo + 1] = b1[q];
+            }
+            S.n_kepler += 1;
+            if (ctx.exhausted) atomicOr(err, (unsigned)DERR_KEPLER_BUDGET);
+        }
+        __syncthreads();
+    }
+}
+
+// SIAnn.dkd / SIAnn.kdk on [lo, lo + n).
+__device__ void sub_evolve(SubState &S, int lo, int n, double tau,
+                           const SubParams &P, const Sweep &acc,
+                           unsigned *err)
+{
+    if (n <= 2) {
+        sub_fewbody(S, lo, n, tau, P, err);
+        return;
+    }
+    for (int k = 0; k < P.seq_len; ++k) {
+        const double c = P.coef[k] * tau;
+        if ((P.outer[k] != 0) != (P.kdk != 0)) {
+            sub_drift(S, lo, n, c);
+        } else {
+            sub_acc(S, lo, n, lo, n, P, acc);
+            sub_kick(S, lo, n, c);
+        }
+    }
+}
+
+// Entry half of SIA.recurse: Tstep, shared-step quantisation, split; pushes
+// the frame (nothing for an empty subsystem).
+__device__ void sub_enter(SubState &S, int lo, int n, double tau,
+                          const SubParams &P, const Sweep &tst)
+{
+    if (n == 0) return;
+    const int t = threadIdx.x, lane = t & 31, w = t >> 5;
+    if (t == 0) {
+        S.n_recurse += 1;
+        if (S.sp >= SUB_DEPTH) S.status = 1;
+        if (S.sp + 1 > S.max_depth) S.max_depth = S.sp + 1;
+        S.tau = tau;
+    }
+    __syncthreads();
+    if (S.status) return;
+    double flag = -1.0;
+    if (P.mode != 's') {
+        flag = 1.0;
+        if (P.split)
+            sub_split_sweep<TstepS>(S, lo, n, lo, n, F_TSTEP, P.eta);
+        else
+            sub_sweep<TstepPair<double>>(S, lo, n, lo, n, F_TSTEP, tst);
+        if (P.mode == 'a') {
+            double v = t < n ? fabs(S.f[F_TSTEP][lo + t]) : INFINITY;
+            for (int o = 16; o > 0; o >>= 1)
+                v = fmin(v, __shfl_xor_sync(0xffffffffu, v, o));
+            if (lane == 0) S.red[w] = v;
+            __syncthreads();
+            if (t == 0) {
+                double m = S.red[0];
+                for (int q = 1; q < SUB_MAX / 32; ++q) m = fmin(m, S.red[q]);
+                S.tau = d_block_tstep(m, S.t_curr, tau);
+            }
+            __syncthreads();
+        }
+    }
+    const double tq = S.tau;
+    const double thr = flag * fabs(tq);
+    int ns = n;
+    if (n > 2 && !(flag < 0 && thr < 0)) {
+        const bool slow = t < n && fabs(S.f[F_TSTEP][lo + t]) > thr;
+        const unsigned b = __ballot_sync(0xffffffffu, slow);
+        if (lane == 0) S.wc[w] = __popc(b);
+        __syncthreads();
+        unsigned before = 0, total = 0;
+        for (int q = 0; q < SUB_MAX / 32; ++q) {
+            before += q < w ? S.wc[q] : 0;
+            total += S.wc[q];
+        }
+        const unsigned rs = before + __popc(b & ((1u << lane) - 1u));
+        if (t < n) {
+            const int dst = slow ? (int)rs : (int)total + (t - (int)rs);
+#pragma unroll
+            for (int f = 0; f < NFIELD; ++f) S.x[f][dst] = S.f[f][lo + t];
+        }
+        __syncthreads();
+        if (t < n)
+#pragma unroll
+            for (int f = 0; f < NFIELD; ++f) S.f[f][lo + t] = S.x[f][t];
+        ns = (int)total;
+        if (t == 0) S.n_partitions += 1;
+    }
+    if (t == 0) {
+        Frame &fr = S.stk[S.sp];
+        fr.lo = lo;
+        fr.n = n;
+        fr.ns = ns;
+        fr.step = 0;
+        fr.sub = 0;
+        fr.tau = tq;
+        S.sp += 1;
+    }
+    __syncthreads();
+}
+
+__global__ void __launch_bounds__(SUB_MAX)
+k_sia_subtree(Fields F, uint64_t base, int n0, double tau0, SubParams P,
+              SubCtl *ctl, unsigned *err)
+{
+    __shared__ SubState S;
+    const int t = threadIdx.x;
+    if (t < n0)
+        for (int f = 0; f < NFIELD; ++f) S.f[f][t] = F.f[f][base + t];
+    if (t == 0) {
+        S.sp = 0;
+        S.t_curr = ctl->t_curr;
+        S.status = 0;
+        S.max_depth = 0;
+        S.n_recurse = S.n_kepler = S.n_partitions = 0;
+        S.interactions = 0;
+    }
+    __syncthreads();
+    Sweep acc, tst;
+    memset(&acc, 0, sizeof(acc));
+    memset(&tst, 0, sizeof(tst));
+    acc.kernel = K_ACC;
+    tst.kernel = K_TSTEP;
+    tst.scal[0] = P.eta;
+
+    sub_enter(S, 0, n0, tau0, P, tst);
+    while (S.sp > 0 && S.status == 0) {
+        const Frame fr = S.stk[S.sp - 1];
+        const int nf = fr.n - fr.ns;
+        __syncthreads();
+        if (fr.step == P.seq_len) {
+            // exit half of SIA.recurse (sia.py:1112-1123)
+            if (t < fr.ns) {
+                const int i = fr.lo + t;
+                S.f[F_TSTEP][i] = fr.tau;
+                S.f[F_TIME][i] = S.f[F_TIME][i] + fr.tau;
+                ((long long *)S.f[F_NSTEP])[i] += 1;
+            }
+            if (t == 0) {
+                if (nf == 0) S.t_curr += fr.tau;
+                S.sp -= 1;
+            }
+            __syncthreads();
+            continue;
+        }
+        const double c = P.coef[fr.step] * fr.tau;
+        if (P.outer[fr.step]) {
+            if (fr.sub == 0) {
+                // sf_drift: evolve the slow part, then recurse into the fast
+                sub_evolve(S, fr.lo, fr.ns, c, P, acc, err);
+                if (t == 0) S.stk[S.sp - 1].sub = 1;
+                __syncthreads();
+                sub_enter(S, fr.lo + fr.ns, nf, c, P, tst);
+                continue;
+            }
+            if (t == 0) {
+                S.stk[S.sp - 1].sub = 0;
+                S.stk[S.sp - 1].step += 1;
+            }
+            __syncthreads();
+            continue;
+        }
+        // sf_kick (sia.py:199-297, Newtonian branch)
+        if (fr.ns && nf) {
+            sub_acc(S, fr.lo, fr.ns, fr.lo + fr.ns, nf, P, acc);
+            sub_acc(S, fr.lo + fr.ns, nf, fr.lo, fr.ns, P, acc);
+            sub_kick(S, fr.lo, fr.ns, c);
+            sub_kick(S, fr.lo + fr.ns, nf, c);
+        }
+        if (t == 0) S.stk[S.sp - 1].step += 1;
+        __syncthreads();
+    }
+    __syncthreads();
+    if (t < n0)
+        for (int f = 0; f < NFIELD; ++f) F.f[f][base + t] = S.f[f][t];
+    if (t == 0) {
+        ctl->t_curr = S.t_curr;
+        ctl->status = S.status;
+        ctl->max_depth = S.max_depth;
+        ctl->n_recurse = S.n_recurse;
+        ctl->n_kepler = S.n_kepler;
+        ctl->n_partitions = S.n_partitions;
+        ctl->interactions = S.interactions;
+    }
+}
+
+// ---------------------------------------------------------------------------
 // Host side.
 // ---------------------------------------------------------------------------
 struct Sia {
@@ -248,8 +652,15 @@ struct Sia {
     double *partial = nullptr;
     int sms = 152;
     long long kepler_budget = 1LL << 20;
+    // subsystems of at most sub_max particles run as one CTA (0: never)
+    int sub_max = SUB_MAX;
+    SubParams P;
+    SubCtl *ctl_dev = nullptr, *ctl_host = nullptr;
     // statistics
     long long n_recurse = 0, n_kepler = 0, n_sweeps = 0, n_partitions = 0;
+    long long n_subtrees = 0;
+    unsigned long long interactions = 0;   // sum of ni * nj over all sums
+    double subtree_s = 0.0;      // wall time inside subtree launches
     int max_depth = 0;
 };
 
@@ -281,6 +692,7 @@ cudaError_t sweep(Sia *S, int kernel, uint64_t ilo, uint64_t ni, uint64_t jlo,
         s.out[o] = S->F.f[first_out + o] + ilo;
     s.scal[0] = kernel == K_TSTEP ? S->eta : 0.0;
     S->n_sweeps += 1;
+    S->interactions += (unsigned long long)ni * nj;
     if (S->sweep_mode == MODE_EXACT)
         return launch_exact<double>(s, S->stream, S->kepler_budget, S->err);
     const int nf = split_nf_host(kernel);
@@ -392,11 +804,43 @@ int read_word(Sia *S, unsigned long long *out)
     return ST_OK;
 }
 
+// The whole of SIA.recurse on [lo, lo + n) in one CTA (n <= SUB_MAX).
+int subtree(Sia *S, uint64_t lo, uint64_t n, double tau, int depth)
+{
+    const auto t0 = std::chrono::steady_clock::now();
+    SubCtl *h = S->ctl_host;
+    memset(h, 0, sizeof(*h));
+    h->t_curr = S->t_curr;
+    if (cudaMemcpyAsync(S->ctl_dev, h, sizeof(*h), cudaMemcpyHostToDevice,
+                        S->stream) != cudaSuccess)
+        return ST_CUDA;
+    k_sia_subtree<<<1, SUB_MAX, 0, S->stream>>>(S->F, lo, (int)n, tau, S->P,
+                                                S->ctl_dev, S->err);
+    g_launch_count += 1;
+    if (cudaGetLastError() != cudaSuccess ||
+        cudaMemcpyAsync(h, S->ctl_dev, sizeof(*h), cudaMemcpyDeviceToHost,
+                        S->stream) != cudaSuccess ||
+        cudaStreamSynchronize(S->stream) != cudaSuccess)
+        return ST_CUDA;
+    S->subtree_s += std::chrono::duration<double>(
+                        std::chrono::steady_clock::now() - t0).count();
+    S->n_subtrees += 1;
+    S->t_curr = h->t_curr;
+    S->n_recurse += h->n_recurse;
+    S->n_kepler += h->n_kepler;
+    S->n_partitions += h->n_partitions;
+    S->interactions += h->interactions;
+    if (depth + h->max_depth - 1 > S->max_depth)
+        S->max_depth = depth + h->max_depth - 1;
+    return h->status ? ST_TOO_LARGE : ST_OK;
+}
+
 // SIA.recurse (sia.py:1097-1123) on the subsystem [lo, lo + n).
 int recurse(Sia *S, uint64_t lo, uint64_t n, double tau, int depth)
 {
     if (n == 0) return ST_OK;
     if (depth > MAX_DEPTH) return ST_TOO_LARGE;
+    if (n <= (uint64_t)S->sub_max) return subtree(S, lo, n, tau, depth);
     S->n_recurse += 1;
     if (depth > S->max_depth) S->max_depth = depth;
     double flag = -1.0;
@@ -456,6 +900,8 @@ void release(Sia *S)
     cudaFree(S->err);
     cudaFree(S->pack);
     cudaFree(S->partial);
+    cudaFree(S->ctl_dev);
+    cudaFreeHost(S->ctl_host);
     if (S->stream) cudaStreamDestroy(S->stream);
     delete S;
 }
@@ -493,6 +939,17 @@ TG_EXPORT int tupan_gb300_sia_create(uint64_t n, const char *method, double eta,
     S->kdk = kdk;
     S->eta = eta;
     S->seq = make_sequence(*sc);
+    memset(&S->P, 0, sizeof(S->P));
+    S->P.seq_len = (int)S->seq.size();
+    for (int k = 0; k < S->P.seq_len && k < SEQ_MAX; ++k) {
+        S->P.outer[k] = S->seq[k].first ? 1 : 0;
+        S->P.coef[k] = S->seq[k].second;
+    }
+    S->P.mode = md;
+    S->P.kdk = kdk ? 1 : 0;
+    S->P.split = mode == MODE_SPLIT ? 1 : 0;
+    S->P.eta = eta;
+    S->P.budget = S->kepler_budget;
     int dev = 0;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&S->sms, cudaDevAttrMultiProcessorCount, dev);
@@ -501,7 +958,9 @@ TG_EXPORT int tupan_gb300_sia_create(uint64_t n, const char *method, double eta,
         cudaStreamCreateWithFlags(&S->stream, cudaStreamNonBlocking) == cudaSuccess &&
         cudaMalloc((void **)&S->pool, 2 * NFIELD * fb) == cudaSuccess &&
         cudaMalloc((void **)&S->word, sizeof(unsigned long long)) == cudaSuccess &&
-        cudaMalloc((void **)&S->err, sizeof(unsigned)) == cudaSuccess;
+        cudaMalloc((void **)&S->err, sizeof(unsigned)) == cudaSuccess &&
+        cudaMalloc((void **)&S->ctl_dev, sizeof(SubCtl)) == cudaSuccess &&
+        cudaMallocHost((void **)&S->ctl_host, sizeof(SubCtl)) == cudaSuccess;
     if (ok && mode == MODE_SPLIT)
         ok = cudaMalloc(&S->pack, 2 * n * 3 * sizeof(float4) + 256) == cudaSuccess &&
              cudaMalloc((void **)&S->partial, 64 * 3 * fb) == cudaSuccess;
@@ -585,7 +1044,10 @@ TG_EXPORT int tupan_gb300_sia_get_state(void *handle, long long *id,
 }
 
 // Counters since creation: stats[0] recursion calls, [1] Kepler solves,
-// [2] force/tstep sweeps, [3] partitions, [4] deepest level, [5] base steps.
+// [2] force/tstep sweeps launched from the host, [3] partitions, [4]
+// deepest level, [5] base steps, [6] single-CTA subtree launches, [7]
+// microseconds spent in them, [8] pair interactions summed (ni * nj of
+// every Acc and Tstep sum).
 TG_EXPORT int tupan_gb300_sia_stats(void *handle, long long *stats)
 {
     Sia *S = (Sia *)handle;
@@ -596,7 +1058,22 @@ TG_EXPORT int tupan_gb300_sia_stats(void *handle, long long *stats)
     stats[3] = S->n_partitions;
     stats[4] = S->max_depth;
     stats[5] = S->steps;
+    stats[6] = S->n_subtrees;
+    stats[7] = (long long)(S->subtree_s * 1e6);
+    stats[8] = (long long)S->interactions;
     return ST_OK;
+}
+
+// Largest subsystem handed whole to the single-CTA recursion kernel
+// (0 .. 128; 0: every level driven from the host).  Both paths give the
+// same bits.  Returns the previous value, or -1 for a bad argument.
+TG_EXPORT int tupan_gb300_sia_set_subtree(void *handle, int max_n)
+{
+    Sia *S = (Sia *)handle;
+    if (!S || max_n < 0 || max_n > SUB_MAX) return -1;
+    const int old = S->sub_max;
+    S->sub_max = max_n;
+    return old;
 }
 
 TG_EXPORT int tupan_gb300_sia_destroy(void *handle)

@@ -396,4 +396,26 @@ __device__ __forceinline__ void pair_state(const R *ip, const R *jp, R *p0,
     *m = ip[0] + jp[0];
 }
 
+// kepler_solver_kernel_common.h:39-79: particles a and b (m r e2 v) evolved
+// over dt in their centre-of-mass frame; a1/b1 receive r and v (6 each) and
+// may alias nothing the caller still needs from a or b.
+template <typename R>
+__device__ void kepler_two_body(const R *a, const R *b, R dt, R *a1, R *b1,
+                                KepCtx<R> &ctx)
+{
+    R p0[6], p1[6], m, e2;
+    pair_state(a, b, p0, &m, &e2);
+    R amu = a[0] / m;
+    R bmu = b[0] / m;
+    R cm[6];
+    for (int c = 0; c < 3; ++c) cm[c] = amu * a[1 + c] + bmu * b[1 + c];
+    for (int c = 0; c < 3; ++c) cm[3 + c] = amu * a[5 + c] + bmu * b[5 + c];
+    for (int c = 0; c < 3; ++c) cm[c] += cm[3 + c] * dt;
+    kep_solve(dt, m, e2, p0, p1, ctx);
+    for (int q = 0; q < 6; ++q) {
+        a1[q] = cm[q] + bmu * p1[q];
+        b1[q] = cm[q] - amu * p1[q];
+    }
+}
+
 }  // namespace tg

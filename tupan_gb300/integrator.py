@@ -201,6 +201,8 @@ def _declare_sia(L):
     L.tupan_gb300_sia_get_state.restype = c.c_int
     L.tupan_gb300_sia_stats.argtypes = [c.c_void_p, lp]
     L.tupan_gb300_sia_stats.restype = c.c_int
+    L.tupan_gb300_sia_set_subtree.argtypes = [c.c_void_p, c.c_int]
+    L.tupan_gb300_sia_set_subtree.restype = c.c_int
     L.tupan_gb300_sia_destroy.argtypes = [c.c_void_p]
     L.tupan_gb300_sia_destroy.restype = c.c_int
 
@@ -265,12 +267,22 @@ class DeviceSIA(object):
             raise lib.TupanGB300Error("sia_get_state failed")
         return out
 
+    def set_subtree(self, max_n):
+        """Subsystems of at most ``max_n`` (<= 128) particles run their
+        whole recursion in one CTA; 0 drives every level from the host.
+        Both give the same bits."""
+        old = self.L.tupan_gb300_sia_set_subtree(self.h, int(max_n))
+        if old < 0:
+            raise ValueError("max_n must be in 0..128")
+        return old
+
     def stats(self):
-        s = np.zeros(6, dtype=np.int64)
+        s = np.zeros(9, dtype=np.int64)
         self.L.tupan_gb300_sia_stats(
             self.h, s.ctypes.data_as(ctypes.POINTER(ctypes.c_longlong)))
         return dict(zip(("recursions", "kepler", "sweeps", "partitions",
-                         "max_depth", "steps"), (int(x) for x in s)))
+                         "max_depth", "steps", "subtrees", "subtree_us",
+                         "interactions"), (int(x) for x in s)))
 
     def close(self):
         if self.h:

@@ -4,8 +4,9 @@ recursion statistics.
     python -m tupan_gb300.sia_bench --n 65536 --method sia21h.dkd --steps 2
 
 Prints one JSON line: base steps, wall time, steps/s, recursion calls,
-sweeps, partitions, deepest level, Kepler solves and the fp64 energy error
-(EXACT Phi on the device).
+sweeps, partitions, deepest level, Kepler solves, the pair interactions
+summed over all levels (and their rate) and the fp64 energy error (EXACT
+Phi on the device).
 """
 
 import argparse
@@ -48,6 +49,7 @@ def main(argv=None):
            "steps_per_s": len(times) / (t1 - t0),
            "dE_over_E": ((k1 + p1) - (k0 + p0)) / abs(k0 + p0)}
     res.update(stats)
+    res["gint_per_s"] = stats["interactions"] / (t1 - t0) / 1e9
     print(json.dumps(res))
 
 
