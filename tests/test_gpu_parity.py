@@ -268,6 +268,24 @@ def test_split_every_variant(variant, gsplit):
     assert ea.max() <= 1e-6, ea.max()
 
 
+@pytest.mark.parametrize("variant", range(7))
+@pytest.mark.parametrize("gsplit", [1, 3])
+def test_split_tstep_every_variant(variant, gsplit):
+    # variants 5 and 6 evaluate two i per thread as packed FP32 pairs
+    ps = ics.plummer(3000, eps=1e-4, seed=15)
+    js = {k: np.ascontiguousarray(v[:2600]) for k, v in ps.items()}
+    sc = {"eta": 1.0 / 64}
+    want = oracle.run("tstep_kernel", ps, js, sc)
+    lib.set_split_config("tstep_kernel", variant, gsplit)
+    try:
+        got = run_gpu("tstep_kernel", ps, js, sc, mode=lib.MODE_SPLIT)
+    finally:
+        lib.set_split_config("tstep_kernel", -1, 0)
+    for g, w in zip(got, want):
+        assert np.all(np.isfinite(g))
+        assert np.max(np.abs(g - w) / w) <= 1e-5
+
+
 @pytest.mark.parametrize("ni,nj", [(1, 1), (1, 5000), (5000, 1), (7, 300),
                                    (513, 257)])
 def test_split_edge_sizes(ni, nj):

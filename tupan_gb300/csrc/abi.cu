@@ -230,10 +230,10 @@ void choose_split(const DeviceState *d, int kernel, uint64_t ni, uint64_t nj,
     for (int v = 0; v < nv; ++v) {
         int nip, js, nt;
         variant_info_any(v, &nip, &js, &nt);
-        // variants 5 and 6 are the packed-pair forms of 0 and (2 i, JS=4):
-        // measured 12-16 % faster on phi/acc/acc_jerk; other kernels would
-        // only repeat a scalar variant under another number.  7 and 8 are 5
-        // and 6 on duplicated j-records.
+        // variants 5 and 6 are the packed-pair forms of 0 and (2 i, JS=4)
+        // for phi/acc/acc_jerk/tstep (measured 12-16 % faster on the first
+        // three); snap_crackle would only repeat a scalar variant under
+        // another number.  7 and 8 are 5 and 6 on duplicated j-records.
         const bool packed = (v >= 5);
         if (packed && !x2) continue;
         const double ipc = (double)(nt / js) * nip;

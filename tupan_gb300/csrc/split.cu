@@ -235,6 +235,57 @@ struct AccJerkS2 {
     }
 };
 
+// Tstep on both lanes (TstepS's arithmetic); the i image also carries m.
+struct PosVelMI2 {
+    float2 nxh, nyh, nzh, nxl, nyl, nzl, e2, nvx, nvy, nvz, m;
+};
+
+__device__ __forceinline__ float2 rsqrt_nr2_raw(float2 s)
+{
+    float2 y = make_float2(rsqrtf(s.x), rsqrtf(s.y));
+    float2 u = mul2(mul2(s, y), y);
+    return mul2(y, fma2(u, dup(-0.5f), dup(1.5f)));
+}
+
+struct TstepS2 {
+    using P = AccJerkS::P;
+    using I = PosVelMI2;
+    __device__ static I pack(const P &a, const P &b)
+    {
+        return {make_float2(-a.xh, -b.xh), make_float2(-a.yh, -b.yh),
+                make_float2(-a.zh, -b.zh), make_float2(-a.xl, -b.xl),
+                make_float2(-a.yl, -b.yl), make_float2(-a.zl, -b.zl),
+                make_float2(a.e2, b.e2),   make_float2(-a.vx, -b.vx),
+                make_float2(-a.vy, -b.vy), make_float2(-a.vz, -b.vz),
+                make_float2(a.m, b.m)};
+    }
+    __device__ static void pair(const I &i, const P &j, float2 *acc, float eta)
+    {
+        float2 dx = add2(add2(dup(j.xh), i.nxh), add2(dup(j.xl), i.nxl));
+        float2 dy = add2(add2(dup(j.yh), i.nyh), add2(dup(j.yl), i.nyl));
+        float2 dz = add2(add2(dup(j.zh), i.nzh), add2(dup(j.zl), i.nzl));
+        float2 ux = add2(dup(j.vx), i.nvx);
+        float2 uy = add2(dup(j.vy), i.nvy);
+        float2 uz = add2(dup(j.vz), i.nvz);
+        float2 h2 = add2(i.e2, dup(j.e2));
+        float2 msum = add2(i.m, dup(j.m));
+        float2 s = fma2(dz, dz, fma2(dy, dy, fma2(dx, dx, h2)));
+        float2 rv = fma2(dz, uz, fma2(dy, uy, mul2(dx, ux)));
+        float2 v2 = fma2(uz, uz, fma2(uy, uy, mul2(ux, ux)));
+        float2 y = rsqrt_nr2_raw(s);
+        float2 q = mul2(y, y);
+        float2 phi = mul2(msum, y);
+        float2 w2 = mul2(q, fma2(dup(2.0f), phi, v2));
+        float2 g = mul2(q, fma2(mul2(dup(2.0f), q), phi, w2));
+        g = mul2(g, mul2(dup(eta), rsqrt_nr2_raw(w2)));
+        w2 = fma2(make_float2(-g.x, -g.y), rv, w2);
+        w2.x = (s.x > h2.x) ? w2.x : 0.0f;
+        w2.y = (s.y > h2.y) ? w2.y : 0.0f;
+        acc[0] = add2(acc[0], w2);
+        acc[1] = make_float2(fmaxf(w2.x, acc[1].x), fmaxf(w2.y, acc[1].y));
+    }
+};
+
 // Duplicated j-record images (variants 7 and 8).
 struct PosJ2 { float2 xh, yh, zh, xl, yl, zl, m, e2; };
 struct PosVelJ2 { float2 xh, yh, zh, xl, yl, zl, vx, vy, vz, m, e2; };
@@ -328,6 +379,7 @@ template <class Op> struct X2Of { using type = void; };
 template <> struct X2Of<PhiS> { using type = PhiS2; };
 template <> struct X2Of<AccS> { using type = AccS2; };
 template <> struct X2Of<AccJerkS> { using type = AccJerkS2; };
+template <> struct X2Of<TstepS> { using type = TstepS2; };
 
 // Duplicated-j partner (variants 7 and 8).
 template <class Op> struct D2Of { using type = void; };
@@ -754,7 +806,7 @@ static const VariantInfo kVariants[] = {
     {1, 4, 256},   // fewer i: lanes share an i and split the j-tile
     {1, 16, 256},
     {1, 32, 128},
-    {2, 1, 256},   // as 0 with packed FP32 pairs (phi, acc, acc_jerk)
+    {2, 1, 256},   // as 0 with packed FP32 pairs (phi, acc, acc_jerk, tstep)
     {2, 4, 256},   // packed, lanes split the j-tile
 };
 constexpr int N_VARIANTS = sizeof(kVariants) / sizeof(kVariants[0]);
@@ -771,7 +823,8 @@ void split_variant_info(int v, int *ni_per_thread, int *jsplit, int *threads)
 // Kernels with a packed-pair (f32x2) operator: variants 5 and 6 use it.
 bool split_has_x2(int kernel)
 {
-    return kernel == K_PHI || kernel == K_ACC || kernel == K_ACC_JERK;
+    return kernel == K_PHI || kernel == K_ACC || kernel == K_ACC_JERK ||
+           kernel == K_TSTEP;
 }
 
 bool split_supported(int kernel)
