@@ -286,6 +286,27 @@ def test_split_tstep_every_variant(variant, gsplit):
         assert np.max(np.abs(g - w) / w) <= 1e-5
 
 
+@pytest.mark.parametrize("variant", range(7))
+@pytest.mark.parametrize("gsplit", [1, 3])
+def test_split_snap_crackle_every_variant(variant, gsplit):
+    ps = ics.plummer(2500, eps=1e-4, seed=16)
+    aj = oracle.run("acc_jerk_kernel", ps, ps)
+    for c, k in zip(("ax", "ay", "az", "jx", "jy", "jz"), aj):
+        ps[c] = k
+    js = {k: np.ascontiguousarray(v[:2200]) for k, v in ps.items()}
+    want = oracle.run("snap_crackle_kernel", ps, js)
+    lib.set_split_config("snap_crackle_kernel", variant, gsplit)
+    try:
+        got = run_gpu("snap_crackle_kernel", ps, js, mode=lib.MODE_SPLIT)
+    finally:
+        lib.set_split_config("snap_crackle_kernel", -1, 0)
+    es = vec_rel_err(got, want, (0, 1, 2))
+    ec = vec_rel_err(got, want, (3, 4, 5))
+    assert np.all(np.isfinite(es)) and np.all(np.isfinite(ec))
+    assert np.median(es) <= 1e-5 and np.median(ec) <= 1e-5, (
+        np.median(es), np.median(ec))
+
+
 @pytest.mark.parametrize("ni,nj", [(1, 1), (1, 5000), (5000, 1), (7, 300),
                                    (513, 257)])
 def test_split_edge_sizes(ni, nj):

@@ -35,7 +35,10 @@ def tune(kernel, ni, nj, reps=3, gsplits=GSPLITS, record=True):
     ps = ics.plummer(max(ni, nj), eps=1e-4, seed=17)
     names = [arg[1:] for (kind, arg) in abi.SIGNATURES[kernel]
              if kind == "in" and arg[0] == "i"]
-    data = {k: torch.from_numpy(np.ascontiguousarray(ps[k])).to(dev)
+    # attributes a Plummer sphere lacks (a, j for snap_crackle) are zero:
+    # the timing does not depend on their values
+    data = {k: torch.from_numpy(np.ascontiguousarray(
+                ps[k] if k in ps else np.zeros(len(ps["m"])))).to(dev)
             for k in names}
     ip = [data[k].data_ptr() for k in names]
     nout = len([1 for (kind, _) in abi.SIGNATURES[kernel] if kind == "out"])
