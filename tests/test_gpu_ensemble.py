@@ -43,3 +43,14 @@ def test_ensemble_systems_of_every_size_finish():
     t, k, _ = ens.state()
     assert np.all(t == 1.0 / 64) and np.all(k >= 1)
     ens.close()
+
+
+def test_ensemble_evolve_in_stages_reaches_each_end_time():
+    # the captured step graph must pick up the t_end of each evolve call
+    systems = make_systems(40, lo=3, hi=200, seed=10)
+    ens = DeviceEnsemble(systems, 1.0 / 64)
+    for t_end in (1.0 / 256, 1.0 / 128, 1.0 / 64):
+        ens.evolve(t_end, batch=4)
+        t, k, _ = ens.state()
+        assert np.all(t == t_end), (t_end, t.min(), t.max())
+    ens.close()

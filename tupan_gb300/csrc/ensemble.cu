@@ -8,7 +8,10 @@
 // systems from an atomic work queue, largest first); the per-particle
 // predictor/corrector and the per-system step control are elementwise
 // kernels.  A step is a fixed launch sequence, so `batch` steps are captured
-// in a CUDA graph and replayed; systems that reached t_end are skipped.
+// in a CUDA graph and replayed.  Each step first compacts the systems that
+// have not reached t_end into a list (largest first); packing, the sweeps
+// and the per-particle kernels walk only that list, so the long tail of a
+// few slow systems costs in proportion to their particles.
 // Energies are fp64: an in-order fp64 Phi per system (same arithmetic and j
 // order as phi_kernel.c) and fp64 sums in fixed order.
 
@@ -22,6 +25,7 @@
 #include <vector>
 
 #include "tg_common.cuh"
+#include "tg_split_ops.cuh"
 
 #define TG_EXPORT extern "C" __attribute__((visibility("default")))
 
@@ -32,7 +36,8 @@ cudaError_t launch_split_batched(int kernel, const float4 *rec,
                                  const uint64_t *off, const unsigned *order,
                                  const int *active, unsigned n_sys,
                                  unsigned *queue, void *const *out, double eta,
-                                 unsigned *err, int sms, cudaStream_t st);
+                                 unsigned *err, int sms, cudaStream_t st,
+                                 const unsigned *n_dev, const uint2 *items);
 }  // namespace tg
 
 using namespace tg;
@@ -76,9 +81,12 @@ __device__ __forceinline__ double e_block_tstep(double min_ts, double t,
     for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;       \
          i < (n); i += (uint64_t)gridDim.x * blockDim.x)
 
-__global__ void k_e_begin(SysCtl *c, int *active, unsigned ns, double t_end,
-                          double eta)
+// t_end lives in device memory: a captured graph replays with the value of
+// the current evolve call.
+__global__ void k_e_begin(SysCtl *c, int *active, unsigned ns,
+                          const double *t_end_p, double eta)
 {
+    const double t_end = *t_end_p;
     GRID_LOOP(s, ns)
     {
         if (fabs(c[s].t) >= t_end) {
@@ -92,14 +100,102 @@ __global__ void k_e_begin(SysCtl *c, int *active, unsigned ns, double t_end,
     }
 }
 
-__global__ void k_e_min(EArrays A, uint64_t n, SysCtl *c, const int *active)
+// The systems still short of t_end, in processing order (largest first): a
+// stable compaction of `order` by the active flags, in one CTA.  Every
+// per-particle kernel below walks this list, so a step costs in proportion
+// to the particles of the active systems, not of the whole ensemble.
+// The batched sweep's work items, in the same order: each active system
+// split into i-blocks of ITEM_IB particles, (system, first i) per item, so
+// a large system is spread over several CTAs (shorter critical path when
+// few systems are left) and the CTAs stay balanced.
+constexpr int COMPACT_NT = 1024;
+constexpr int ITEM_IB = 128;     // the batched sweep's i-block (BATCH_IB)
+
+__device__ unsigned block_exclusive_scan(unsigned v, unsigned *wsum,
+                                         unsigned *total)
 {
-    GRID_LOOP(i, n)
+    const int t = threadIdx.x, lane = t & 31, w = t >> 5;
+    unsigned x = v;
+    for (int o = 1; o < 32; o <<= 1) {
+        const unsigned y = __shfl_up_sync(0xffffffffu, x, o);
+        if (lane >= o) x += y;
+    }
+    if (lane == 31) wsum[w] = x;
+    __syncthreads();
+    unsigned before = 0, all = 0;
+    for (int q = 0; q < COMPACT_NT / 32; ++q) {
+        before += q < w ? wsum[q] : 0;
+        all += wsum[q];
+    }
+    __syncthreads();
+    *total = all;
+    return before + x - v;
+}
+
+__global__ void __launch_bounds__(COMPACT_NT)
+k_e_compact(const unsigned *order, const int *active, const uint64_t *off,
+            unsigned ns, unsigned *alist, unsigned *acount, uint2 *items,
+            unsigned *icount)
+{
+    __shared__ unsigned wsum[COMPACT_NT / 32];
+    const int t = threadIdx.x;
+    unsigned sbase = 0, ibase = 0;
+    for (unsigned c0 = 0; c0 < ns; c0 += COMPACT_NT) {
+        const unsigned k = c0 + t;
+        const unsigned s = k < ns ? order[k] : 0;
+        const bool on = k < ns && active[s];
+        const unsigned n = on ? (unsigned)(off[s + 1] - off[s]) : 0;
+        const unsigned nb = on ? (n + ITEM_IB - 1) / ITEM_IB : 0;
+        unsigned stot, itot;
+        const unsigned spos = block_exclusive_scan(on ? 1u : 0u, wsum, &stot);
+        const unsigned ipos = block_exclusive_scan(nb, wsum, &itot);
+        if (on) {
+            alist[sbase + spos] = s;
+            for (unsigned q = 0; q < nb; ++q)
+                items[ibase + ipos + q] = make_uint2(s, q * ITEM_IB);
+        }
+        sbase += stot;
+        ibase += itot;
+    }
+    if (t == 0) {
+        *acount = sbase;
+        *icount = ibase;
+    }
+}
+
+// for each active system s (CTA-strided over the list): i over its particles
+#define ACTIVE_LOOP(s, i, alist, acount, off)                                  \
+    for (unsigned a_ = blockIdx.x; a_ < *(acount); a_ += gridDim.x)          \
+        for (uint64_t s = (alist)[a_], i = (off)[s] + threadIdx.x;           \
+             i < (off)[s + 1]; i += blockDim.x)
+
+__global__ void k_e_min(EArrays A, const uint64_t *off, SysCtl *c,
+                        const unsigned *alist, const unsigned *acount)
+{
+    ACTIVE_LOOP(s, i, alist, acount, off)
     {
-        const unsigned s = A.sys[i];
-        if (!active[s]) continue;
         atomicMin(&c[s].min_bits,
                   (unsigned long long)__double_as_longlong(fabs(A.dt[0][i])));
+    }
+}
+
+// Packed records of the active systems (the layout of split.cu's
+// pack_records for 3 float4: {xh yh zh m} {xl yl zl e2} {vx vy vz 0}).
+__global__ void k_e_pack(EArrays A, double *const *rr, double *const *vv,
+                         float4 *out, const uint64_t *off,
+                         const unsigned *alist, const unsigned *acount)
+{
+    ACTIVE_LOOP(s, i, alist, acount, off)
+    {
+        float xh, xl, yh, yl, zh, zl;
+        split2(rr[0][i], xh, xl);
+        split2(rr[1][i], yh, yl);
+        split2(rr[2][i], zh, zl);
+        float4 *r = out + i * 3;
+        r[0] = make_float4(xh, yh, zh, (float)A.m[i]);
+        r[1] = make_float4(xl, yl, zl, (float)A.e2[i]);
+        r[2] = make_float4((float)vv[0][i], (float)vv[1][i], (float)vv[2][i],
+                           0.f);
     }
 }
 
@@ -113,11 +209,11 @@ __global__ void k_e_block(SysCtl *c, const int *active, unsigned ns)
     }
 }
 
-__global__ void k_e_copy(EArrays A, uint64_t n, const int *active)
+__global__ void k_e_copy(EArrays A, const uint64_t *off,
+                         const unsigned *alist, const unsigned *acount)
 {
-    GRID_LOOP(i, n)
+    ACTIVE_LOOP(s, i, alist, acount, off)
     {
-        if (!active[A.sys[i]]) continue;
         for (int d = 0; d < 3; ++d) {
             A.r0[d][i] = A.r[d][i];
             A.v0[d][i] = A.v[d][i];
@@ -126,13 +222,11 @@ __global__ void k_e_copy(EArrays A, uint64_t n, const int *active)
 }
 
 // H4.epredict (hermite.py:83-88)
-__global__ void k_e_predict(EArrays A, uint64_t n, const SysCtl *c,
-                            const int *active)
+__global__ void k_e_predict(EArrays A, const uint64_t *off, const SysCtl *c,
+                            const unsigned *alist, const unsigned *acount)
 {
-    GRID_LOOP(i, n)
+    ACTIVE_LOOP(s, i, alist, acount, off)
     {
-        const unsigned s = A.sys[i];
-        if (!active[s]) continue;
         const double tau = c[s].tau;
         for (int d = 0; d < 3; ++d) {
             const double a = A.f0[d][i], j = A.f0[3 + d][i], v = A.v[d][i];
@@ -143,13 +237,11 @@ __global__ void k_e_predict(EArrays A, uint64_t n, const SysCtl *c,
 }
 
 // H4.ecorrect (hermite.py:96-119)
-__global__ void k_e_correct(EArrays A, uint64_t n, const SysCtl *c,
-                            const int *active)
+__global__ void k_e_correct(EArrays A, const uint64_t *off, const SysCtl *c,
+                            const unsigned *alist, const unsigned *acount)
 {
-    GRID_LOOP(i, n)
+    ACTIVE_LOOP(s, i, alist, acount, off)
     {
-        const unsigned s = A.sys[i];
-        if (!active[s]) continue;
         const double tau = c[s].tau;
         for (int d = 0; d < 3; ++d) {
             const double a0 = A.f0[d][i], a1 = A.f1[d][i];
@@ -224,12 +316,18 @@ struct Ensemble {
     uint64_t *off = nullptr;
     unsigned *order = nullptr;
     int *active = nullptr;
+    unsigned *alist = nullptr;      // active systems, largest first
+    unsigned *acount = nullptr;
+    uint2 *items = nullptr;         // their i-blocks, same order
+    unsigned *icount = nullptr;
+    double **rv_ptrs = nullptr;     // device copies of {r, v}, {r0, v0}
     SysCtl *ctl = nullptr;
     unsigned *queue = nullptr;
     unsigned *err = nullptr;
     float4 *pack = nullptr;
     double *ke = nullptr, *pe = nullptr;
     double t_end = 0.0;
+    double *d_tend = nullptr;       // t_end of the current evolve call
     cudaGraphExec_t graph = nullptr;
     int graph_batch = -1;
     unsigned long long launches_per_batch = 0;
@@ -242,38 +340,51 @@ unsigned grid_for(uint64_t n, int sms)
     return (unsigned)(b < 1 ? 1 : (b > cap ? cap : b));
 }
 
-cudaError_t e_forces(Ensemble *E, double *const *rr, double *const *vv,
-                     double *const *out, int kernel, double eta)
+// One force evaluation of every active system: pack their records, then
+// one persistent batched sweep over the active list.  which = 0: the
+// current state (r, v); 1: the saved state (r0, v0).
+cudaError_t e_forces(Ensemble *E, int which, double *const *out, int kernel,
+                     double eta)
 {
-    const void *at[8] = {E->A.m, rr[0], rr[1], rr[2], E->A.e2, vv[0], vv[1],
-                         vv[2]};
-    cudaError_t e = launch_pack(kernel, E->n, at, E->pack, E->stream);
+    double *const *rr = E->rv_ptrs + 6 * which;
+    k_e_pack<<<E->sms * 4, 256, 0, E->stream>>>(E->A, rr, rr + 3, E->pack,
+                                                E->off, E->alist, E->acount);
+    g_launch_count += 1;
+    cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) return e;
-    return launch_split_batched(kernel, E->pack, E->off, E->order, E->active,
+    return launch_split_batched(kernel, E->pack, E->off, E->alist, E->active,
                                 E->ns, E->queue, (void *const *)out, eta,
-                                E->err, E->sms, E->stream);
+                                E->err, E->sms, E->stream, E->icount,
+                                E->items);
 }
 
 cudaError_t e_step(Ensemble *E)
 {
     cudaStream_t st = E->stream;
-    const unsigned gp = grid_for(E->n, E->sms), gs = grid_for(E->ns, E->sms);
-    k_e_begin<<<gs, 256, 0, st>>>(E->ctl, E->active, E->ns, E->t_end, E->eta);
-    cudaError_t e = e_forces(E, E->A.r, E->A.v, E->A.dt, K_TSTEP, E->eta);
+    const unsigned gs = grid_for(E->ns, E->sms);
+    const unsigned ga = (unsigned)E->sms * 4;   // CTAs over active systems
+    k_e_begin<<<gs, 256, 0, st>>>(E->ctl, E->active, E->ns, E->d_tend,
+                                  E->eta);
+    k_e_compact<<<1, COMPACT_NT, 0, st>>>(E->order, E->active, E->off, E->ns,
+                                          E->alist, E->acount, E->items,
+                                          E->icount);
+    cudaError_t e = e_forces(E, 0, E->A.dt, K_TSTEP, E->eta);
     if (e != cudaSuccess) return e;
-    k_e_min<<<gp, 256, 0, st>>>(E->A, E->n, E->ctl, E->active);
+    k_e_min<<<ga, 256, 0, st>>>(E->A, E->off, E->ctl, E->alist, E->acount);
     k_e_block<<<gs, 256, 0, st>>>(E->ctl, E->active, E->ns);
-    k_e_copy<<<gp, 256, 0, st>>>(E->A, E->n, E->active);
-    e = e_forces(E, E->A.r0, E->A.v0, E->A.f0, K_ACC_JERK, 0.0);
+    k_e_copy<<<ga, 256, 0, st>>>(E->A, E->off, E->alist, E->acount);
+    e = e_forces(E, 1, E->A.f0, K_ACC_JERK, 0.0);
     if (e != cudaSuccess) return e;
-    k_e_predict<<<gp, 256, 0, st>>>(E->A, E->n, E->ctl, E->active);
+    k_e_predict<<<ga, 256, 0, st>>>(E->A, E->off, E->ctl, E->alist,
+                                    E->acount);
     for (int pass = 0; pass < 2; ++pass) {
-        e = e_forces(E, E->A.r, E->A.v, E->A.f1, K_ACC_JERK, 0.0);
+        e = e_forces(E, 0, E->A.f1, K_ACC_JERK, 0.0);
         if (e != cudaSuccess) return e;
-        k_e_correct<<<gp, 256, 0, st>>>(E->A, E->n, E->ctl, E->active);
+        k_e_correct<<<ga, 256, 0, st>>>(E->A, E->off, E->ctl, E->alist,
+                                        E->acount);
     }
     k_e_end<<<gs, 256, 0, st>>>(E->ctl, E->active, E->ns);
-    g_launch_count += 8;
+    g_launch_count += 9;
     return cudaGetLastError();
 }
 
@@ -344,8 +455,20 @@ TG_EXPORT int tupan_gb300_ensemble_create(unsigned n_sys,
         cudaMalloc((void **)&E->err, sizeof(unsigned)) != cudaSuccess ||
         cudaMalloc((void **)&E->pack, n * 3 * sizeof(float4)) != cudaSuccess ||
         cudaMalloc((void **)&E->ke, n_sys * sizeof(double)) != cudaSuccess ||
-        cudaMalloc((void **)&E->pe, n_sys * sizeof(double)) != cudaSuccess)
+        cudaMalloc((void **)&E->pe, n_sys * sizeof(double)) != cudaSuccess ||
+        cudaMalloc((void **)&E->alist, n_sys * sizeof(unsigned)) != cudaSuccess ||
+        cudaMalloc((void **)&E->acount, sizeof(unsigned)) != cudaSuccess ||
+        cudaMalloc((void **)&E->items,
+                   (size_t)n_sys * (512 / ITEM_IB) * sizeof(uint2)) != cudaSuccess ||
+        cudaMalloc((void **)&E->icount, sizeof(unsigned)) != cudaSuccess ||
+        cudaMalloc((void **)&E->d_tend, sizeof(double)) != cudaSuccess ||
+        cudaMalloc((void **)&E->rv_ptrs, 12 * sizeof(double *)) != cudaSuccess)
         return ST_CUDA;
+    double *rv[12] = {A.r[0],  A.r[1],  A.r[2],  A.v[0],  A.v[1],  A.v[2],
+                      A.r0[0], A.r0[1], A.r0[2], A.v0[0], A.v0[1], A.v0[2]};
+    cudaMemcpy(E->rv_ptrs, rv, sizeof(rv), cudaMemcpyHostToDevice);
+    cudaMemset(E->acount, 0, sizeof(unsigned));
+    cudaMemset(E->icount, 0, sizeof(unsigned));
     cudaMemcpy(A.sys, sys.data(), n * sizeof(unsigned), cudaMemcpyHostToDevice);
     cudaMemcpy(E->off, sys_off, (n_sys + 1) * sizeof(uint64_t),
                cudaMemcpyHostToDevice);
@@ -373,6 +496,9 @@ TG_EXPORT int tupan_gb300_ensemble_evolve(void *handle, double t_end, int batch,
     if (!E) return ST_BAD_ARGUMENT;
     if (batch < 1) batch = 1;
     E->t_end = t_end;
+    if (cudaMemcpy(E->d_tend, &t_end, sizeof(double), cudaMemcpyHostToDevice) !=
+        cudaSuccess)
+        return ST_CUDA;
     if (E->graph && E->graph_batch != batch) {
         cudaGraphExecDestroy(E->graph);
         E->graph = nullptr;
@@ -397,14 +523,22 @@ TG_EXPORT int tupan_gb300_ensemble_evolve(void *handle, double t_end, int batch,
         g_launch_count -= E->launches_per_batch;
     }
     std::vector<SysCtl> c(E->ns);
+    long long last_steps = -1;
     for (;;) {
         if (cudaMemcpy(c.data(), E->ctl, E->ns * sizeof(SysCtl),
                        cudaMemcpyDeviceToHost) != cudaSuccess)
             return ST_CUDA;
         bool all = true;
-        for (unsigned s = 0; s < E->ns && all; ++s)
+        long long steps = 0;
+        for (unsigned s = 0; s < E->ns; ++s) {
             if (fabs(c[s].t) < t_end) all = false;
+            steps += c[s].nsteps;
+        }
         if (all) break;
+        // every replay advances each unfinished system by `batch` steps;
+        // no progress means the device state is not what the graph expects
+        if (steps == last_steps) return ST_DEVICE;
+        last_steps = steps;
         if (cudaGraphLaunch(E->graph, E->stream) != cudaSuccess) return ST_CUDA;
         g_launch_count += E->launches_per_batch;
         if (cudaStreamSynchronize(E->stream) != cudaSuccess) return ST_CUDA;
@@ -467,6 +601,12 @@ TG_EXPORT int tupan_gb300_ensemble_destroy(void *handle)
     cudaFree(E->A.sys);
     cudaFree(E->off);
     cudaFree(E->order);
+    cudaFree(E->alist);
+    cudaFree(E->acount);
+    cudaFree(E->items);
+    cudaFree(E->icount);
+    cudaFree(E->d_tend);
+    cudaFree(E->rv_ptrs);
     cudaFree(E->active);
     cudaFree(E->ctl);
     cudaFree(E->queue);

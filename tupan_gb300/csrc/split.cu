@@ -742,6 +742,9 @@ struct BatchLaunch {
     const unsigned *order;    // systems in processing order
     const int *active;        // per system (may be null: all active)
     unsigned n_sys;
+    const unsigned *n_dev;    // if set: item count in device memory
+    const uint2 *items;       // if set: (system, first i) of each item, an
+                              // i-block of at most BATCH_IB particles
     unsigned *queue;          // work counter (zeroed before the launch)
     double *out[MAX_OUT];
     float eta;
@@ -751,6 +754,7 @@ struct BatchLaunch {
 
 constexpr int BATCH_NT = 256;
 constexpr int BATCH_MAXN = 512;           // largest system held in smem
+constexpr int BATCH_IB = 128;             // i-block of an item
 
 template <class Op>
 __global__ void __launch_bounds__(BATCH_NT, 2)
@@ -766,19 +770,24 @@ split_sweep_batched(const BatchLaunch L)
         mbar_init_fence();
     }
     __syncthreads();
+    const unsigned n_items = L.n_dev ? *L.n_dev : L.n_sys;
     uint32_t phase = 0;
     for (;;) {
         if (tid == 0) item = atomicAdd(L.queue, 1u);
         __syncthreads();
         const unsigned w = item;
-        if (w >= L.n_sys) break;
-        const unsigned sys = L.order[w];
+        if (w >= n_items) break;
+        const unsigned sys = L.items ? L.items[w].x : L.order[w];
         if (L.active && !L.active[sys]) {
             __syncthreads();
             continue;
         }
         const uint64_t b = L.off[sys];
         const int n = (int)(L.off[sys + 1] - b);
+        // i-range of this item: an i-block, or the whole system
+        const int ib = L.items ? (int)L.items[w].y : 0;
+        const int ie = L.items ? (ib + BATCH_IB < n ? ib + BATCH_IB : n) : n;
+        const int ni = ie - ib;
         if (n > BATCH_MAXN) {
             if (tid == 0) atomicOr(L.err, (unsigned)DERR_BAD_LAUNCH);
             __syncthreads();
@@ -794,11 +803,11 @@ split_sweep_batched(const BatchLaunch L)
         if (!__syncthreads_and(got)) break;
         // lanes per i: enough to occupy the block, at most 32
         int lanes = 1;
-        while (lanes < 32 && lanes * 2 * n <= BATCH_NT) lanes *= 2;
+        while (lanes < 32 && lanes * 2 * ni <= BATCH_NT) lanes *= 2;
         const int groups = BATCH_NT / lanes;
         const int lane = tid % lanes;
-        for (int i0 = tid / lanes; i0 - tid / lanes < n; i0 += groups) {
-            const int i = i0 < n ? i0 : n - 1;
+        for (int k0 = tid / lanes; k0 - tid / lanes < ni; k0 += groups) {
+            const int i = ib + (k0 < ni ? k0 : ni - 1);
             const typename Op::P ip = Op::load(rec + i * NF);
             float sum[NO], corr[NO], part[NO];
 #pragma unroll
@@ -829,7 +838,7 @@ split_sweep_batched(const BatchLaunch L)
                     v[c] = (c == MAXC) ? fmax(v[c], u) : v[c] + u;
                 }
             }
-            if (lane == 0 && i0 < n) {
+            if (lane == 0 && k0 < ni) {
                 Op::finish(v, L.eta_d);
 #pragma unroll
                 for (int c = 0; c < NO; ++c) L.out[c][b + i] = v[c];
@@ -843,14 +852,17 @@ cudaError_t launch_split_batched(int kernel, const float4 *rec,
                                  const uint64_t *off, const unsigned *order,
                                  const int *active, unsigned n_sys,
                                  unsigned *queue, void *const *out, double eta,
-                                 unsigned *err, int sms, cudaStream_t st)
+                                 unsigned *err, int sms, cudaStream_t st,
+                                 const unsigned *n_dev, const uint2 *items)
 {
     BatchLaunch L;
+    L.items = items;
     L.rec = rec;
     L.off = off;
     L.order = order;
     L.active = active;
     L.n_sys = n_sys;
+    L.n_dev = n_dev;
     L.queue = queue;
     for (int c = 0; c < MAX_OUT; ++c)
         L.out[c] = c < n_out(kernel) ? (double *)out[c] : nullptr;
@@ -859,7 +871,12 @@ cudaError_t launch_split_batched(int kernel, const float4 *rec,
     L.err = err;
     cudaError_t e = cudaMemsetAsync(queue, 0, sizeof(unsigned), st);
     if (e != cudaSuccess) return e;
-    const unsigned grid = (unsigned)(sms * 2 < (int)n_sys ? sms * 2 : n_sys);
+    // persistent CTAs; with i-block items a system can occupy up to
+    // BATCH_MAXN / BATCH_IB of them
+    const uint64_t max_items =
+        (uint64_t)n_sys * (items ? BATCH_MAXN / BATCH_IB : 1);
+    const unsigned grid =
+        (unsigned)((uint64_t)sms * 2 < max_items ? (uint64_t)sms * 2 : max_items);
     if (grid == 0) return cudaSuccess;
     switch (kernel) {
     case K_ACC: split_sweep_batched<AccS><<<grid, BATCH_NT, 0, st>>>(L); break;
