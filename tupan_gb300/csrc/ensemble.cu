@@ -7,11 +7,15 @@
 // SPLIT sweep (split_sweep_batched: a persistent kernel whose CTAs take
 // systems from an atomic work queue, largest first); the per-particle
 // predictor/corrector and the per-system step control are elementwise
-// kernels.  A step is a fixed launch sequence, so `batch` steps are captured
-// in a CUDA graph and replayed.  Each step first compacts the systems that
-// have not reached t_end into a list (largest first); packing, the sweeps
-// and the per-particle kernels walk only that list, so the long tail of a
-// few slow systems costs in proportion to their particles.
+// kernels.  A step is a fixed sequence of nine launches, so `batch` steps
+// are captured in a CUDA graph and replayed.  Each step first compacts the
+// systems that have not reached t_end into a list (largest first) and
+// splits them into (system, i-block) work items; the sweeps and the
+// per-system kernels walk only that list, and the kernel that produces a
+// state also packs the FP32 records the next sweep reads.  A run is
+// usually dominated by a few systems with hard binaries that need
+// thousands of tiny shared steps, so the step latency with few active
+// systems is what these fusions shorten.
 // Energies are fp64: an in-order fp64 Phi per system (same arithmetic and j
 // order as phi_kernel.c) and fp64 sums in fixed order.
 
@@ -30,8 +34,6 @@
 #define TG_EXPORT extern "C" __attribute__((visibility("default")))
 
 namespace tg {
-cudaError_t launch_pack(int kernel, uint64_t n, const void *const *attrs,
-                        float4 *out, cudaStream_t st);
 cudaError_t launch_split_batched(int kernel, const float4 *rec,
                                  const uint64_t *off, const unsigned *order,
                                  const int *active, unsigned n_sys,
@@ -77,39 +79,16 @@ __device__ __forceinline__ double e_block_tstep(double min_ts, double t,
     return min_bts;
 }
 
-#define GRID_LOOP(i, n)                                                       \
-    for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;       \
-         i < (n); i += (uint64_t)gridDim.x * blockDim.x)
-
-// t_end lives in device memory: a captured graph replays with the value of
-// the current evolve call.
-__global__ void k_e_begin(SysCtl *c, int *active, unsigned ns,
-                          const double *t_end_p, double eta)
-{
-    const double t_end = *t_end_p;
-    GRID_LOOP(s, ns)
-    {
-        if (fabs(c[s].t) >= t_end) {
-            active[s] = 0;
-            c[s].tau = 0.0;
-            continue;
-        }
-        active[s] = 1;
-        c[s].tau = e_base_tstep(c[s].t, t_end, eta);
-        c[s].min_bits = 0x7ff0000000000000ull;
-    }
-}
-
-// The systems still short of t_end, in processing order (largest first): a
-// stable compaction of `order` by the active flags, in one CTA.  Every
-// per-particle kernel below walks this list, so a step costs in proportion
-// to the particles of the active systems, not of the whole ensemble.
-// The batched sweep's work items, in the same order: each active system
-// split into i-blocks of ITEM_IB particles, (system, first i) per item, so
-// a large system is spread over several CTAs (shorter critical path when
-// few systems are left) and the CTAs stay balanced.
+// The systems still short of t_end, in processing order (largest first),
+// and the batched sweep's work items in the same order: each active system
+// split into i-blocks, (system, ib | ie << 16) per item, so a large system
+// is spread over several CTAs.  The block is 128 i while the active systems
+// outnumber the sweep's CTAs (fewer items, less reloading of j-records),
+// and shrinks to 64 and 32 i as systems finish, so the last few systems
+// still use many SMs.  One CTA: the per-system step start (activity, base
+// step; t_end is read from device memory, so a captured graph replays with
+// the value of the current evolve call), then a stable compaction.
 constexpr int COMPACT_NT = 1024;
-constexpr int ITEM_IB = 128;     // the batched sweep's i-block (BATCH_IB)
 
 __device__ unsigned block_exclusive_scan(unsigned v, unsigned *wsum,
                                          unsigned *total)
@@ -133,26 +112,44 @@ __device__ unsigned block_exclusive_scan(unsigned v, unsigned *wsum,
 }
 
 __global__ void __launch_bounds__(COMPACT_NT)
-k_e_compact(const unsigned *order, const int *active, const uint64_t *off,
-            unsigned ns, unsigned *alist, unsigned *acount, uint2 *items,
-            unsigned *icount)
+k_e_begin(SysCtl *c, int *active, const unsigned *order, const uint64_t *off,
+          unsigned ns, const double *t_end_p, double eta, unsigned ctas,
+          unsigned *alist, unsigned *acount, uint2 *items, unsigned *icount)
 {
     __shared__ unsigned wsum[COMPACT_NT / 32];
+    __shared__ unsigned n_active;
     const int t = threadIdx.x;
+    const double t_end = *t_end_p;
+    if (t == 0) n_active = 0;
+    __syncthreads();
+    unsigned mine = 0;
+    for (unsigned s = t; s < ns; s += COMPACT_NT) {
+        const bool on = fabs(c[s].t) < t_end;
+        active[s] = on ? 1 : 0;
+        c[s].tau = on ? e_base_tstep(c[s].t, t_end, eta) : 0.0;
+        mine += on ? 1u : 0u;
+    }
+    for (int o = 16; o > 0; o >>= 1) mine += __shfl_xor_sync(0xffffffffu, mine, o);
+    if ((t & 31) == 0) atomicAdd(&n_active, mine);
+    __syncthreads();
+    const unsigned na = n_active;
+    const unsigned IB = na >= ctas ? 128u : (na >= ctas / 4 ? 64u : 32u);
     unsigned sbase = 0, ibase = 0;
     for (unsigned c0 = 0; c0 < ns; c0 += COMPACT_NT) {
         const unsigned k = c0 + t;
         const unsigned s = k < ns ? order[k] : 0;
         const bool on = k < ns && active[s];
         const unsigned n = on ? (unsigned)(off[s + 1] - off[s]) : 0;
-        const unsigned nb = on ? (n + ITEM_IB - 1) / ITEM_IB : 0;
+        const unsigned nb = on ? (n + IB - 1) / IB : 0;
         unsigned stot, itot;
         const unsigned spos = block_exclusive_scan(on ? 1u : 0u, wsum, &stot);
         const unsigned ipos = block_exclusive_scan(nb, wsum, &itot);
         if (on) {
             alist[sbase + spos] = s;
-            for (unsigned q = 0; q < nb; ++q)
-                items[ibase + ipos + q] = make_uint2(s, q * ITEM_IB);
+            for (unsigned q = 0; q < nb; ++q) {
+                const unsigned ib = q * IB, ie = ib + IB < n ? ib + IB : n;
+                items[ibase + ipos + q] = make_uint2(s, ib | (ie << 16));
+            }
         }
         sbase += stot;
         ibase += itot;
@@ -163,104 +160,110 @@ k_e_compact(const unsigned *order, const int *active, const uint64_t *off,
     }
 }
 
-// for each active system s (CTA-strided over the list): i over its particles
-#define ACTIVE_LOOP(s, i, alist, acount, off)                                  \
+// Packed record of particle i (the layout of split.cu's pack_records for 3
+// float4: {xh yh zh m} {xl yl zl e2} {vx vy vz 0}), from the current state.
+__device__ __forceinline__ void e_pack_one(const EArrays &A, float4 *out,
+                                           uint64_t i)
+{
+    float xh, xl, yh, yl, zh, zl;
+    split2(A.r[0][i], xh, xl);
+    split2(A.r[1][i], yh, yl);
+    split2(A.r[2][i], zh, zl);
+    float4 *r = out + i * 3;
+    r[0] = make_float4(xh, yh, zh, (float)A.m[i]);
+    r[1] = make_float4(xl, yl, zl, (float)A.e2[i]);
+    r[2] = make_float4((float)A.v[0][i], (float)A.v[1][i], (float)A.v[2][i],
+                       0.f);
+}
+
+// Records of every particle (before the first step of an evolve call).
+__global__ void k_e_pack_all(EArrays A, uint64_t n, float4 *out)
+{
+    for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n;
+         i += (uint64_t)gridDim.x * blockDim.x)
+        e_pack_one(A, out, i);
+}
+
+// One CTA per active system (strided over the list).
+#define FOR_ACTIVE_SYSTEM(s, b, e, alist, acount, off)                        \
     for (unsigned a_ = blockIdx.x; a_ < *(acount); a_ += gridDim.x)          \
-        for (uint64_t s = (alist)[a_], i = (off)[s] + threadIdx.x;           \
-             i < (off)[s + 1]; i += blockDim.x)
+        for (uint64_t s = (alist)[a_], b = (off)[s], e = (off)[s + 1]; s != ~0ull; \
+             s = ~0ull)
 
-__global__ void k_e_min(EArrays A, const uint64_t *off, SysCtl *c,
-                        const unsigned *alist, const unsigned *acount)
+// min |dt_a| of the system -> power-of-two step (integrator/__init__.py:
+// 59-78), and the copy of the state at the start of the step.
+__global__ void k_e_step_size(EArrays A, const uint64_t *off, SysCtl *c,
+                              const unsigned *alist, const unsigned *acount)
 {
-    ACTIVE_LOOP(s, i, alist, acount, off)
+    __shared__ double red[8];
+    const int t = threadIdx.x;
+    FOR_ACTIVE_SYSTEM(s, b, e, alist, acount, off)
     {
-        atomicMin(&c[s].min_bits,
-                  (unsigned long long)__double_as_longlong(fabs(A.dt[0][i])));
-    }
-}
-
-// Packed records of the active systems (the layout of split.cu's
-// pack_records for 3 float4: {xh yh zh m} {xl yl zl e2} {vx vy vz 0}).
-__global__ void k_e_pack(EArrays A, double *const *rr, double *const *vv,
-                         float4 *out, const uint64_t *off,
-                         const unsigned *alist, const unsigned *acount)
-{
-    ACTIVE_LOOP(s, i, alist, acount, off)
-    {
-        float xh, xl, yh, yl, zh, zl;
-        split2(rr[0][i], xh, xl);
-        split2(rr[1][i], yh, yl);
-        split2(rr[2][i], zh, zl);
-        float4 *r = out + i * 3;
-        r[0] = make_float4(xh, yh, zh, (float)A.m[i]);
-        r[1] = make_float4(xl, yl, zl, (float)A.e2[i]);
-        r[2] = make_float4((float)vv[0][i], (float)vv[1][i], (float)vv[2][i],
-                           0.f);
-    }
-}
-
-__global__ void k_e_block(SysCtl *c, const int *active, unsigned ns)
-{
-    GRID_LOOP(s, ns)
-    {
-        if (!active[s]) continue;
-        const double m = __longlong_as_double((long long)c[s].min_bits);
-        c[s].tau = e_block_tstep(m, c[s].t, c[s].tau);
-    }
-}
-
-__global__ void k_e_copy(EArrays A, const uint64_t *off,
-                         const unsigned *alist, const unsigned *acount)
-{
-    ACTIVE_LOOP(s, i, alist, acount, off)
-    {
-        for (int d = 0; d < 3; ++d) {
-            A.r0[d][i] = A.r[d][i];
-            A.v0[d][i] = A.v[d][i];
+        double m = INFINITY;
+        for (uint64_t i = b + t; i < e; i += blockDim.x) {
+            m = fmin(m, fabs(A.dt[0][i]));
+            for (int d = 0; d < 3; ++d) {
+                A.r0[d][i] = A.r[d][i];
+                A.v0[d][i] = A.v[d][i];
+            }
         }
+        for (int o = 16; o > 0; o >>= 1)
+            m = fmin(m, __shfl_xor_sync(0xffffffffu, m, o));
+        if ((t & 31) == 0) red[t >> 5] = m;
+        __syncthreads();
+        if (t == 0) {
+            for (int q = 1; q < (int)(blockDim.x >> 5); ++q) m = fmin(m, red[q]);
+            m = fmin(m, red[0]);
+            c[s].tau = e_block_tstep(m, c[s].t, c[s].tau);
+        }
+        __syncthreads();
     }
 }
 
-// H4.epredict (hermite.py:83-88)
+// H4.epredict (hermite.py:83-88), then the records of the predicted state.
 __global__ void k_e_predict(EArrays A, const uint64_t *off, const SysCtl *c,
-                            const unsigned *alist, const unsigned *acount)
+                            float4 *rec, const unsigned *alist,
+                            const unsigned *acount)
 {
-    ACTIVE_LOOP(s, i, alist, acount, off)
+    FOR_ACTIVE_SYSTEM(s, b, e, alist, acount, off)
     {
         const double tau = c[s].tau;
-        for (int d = 0; d < 3; ++d) {
-            const double a = A.f0[d][i], j = A.f0[3 + d][i], v = A.v[d][i];
-            A.r[d][i] = A.r[d][i] + ((j * tau / 3 + a) * tau / 2 + v) * tau;
-            A.v[d][i] = v + (j * tau / 2 + a) * tau;
+        for (uint64_t i = b + threadIdx.x; i < e; i += blockDim.x) {
+            for (int d = 0; d < 3; ++d) {
+                const double a = A.f0[d][i], j = A.f0[3 + d][i], v = A.v[d][i];
+                A.r[d][i] = A.r[d][i] + ((j * tau / 3 + a) * tau / 2 + v) * tau;
+                A.v[d][i] = v + (j * tau / 2 + a) * tau;
+            }
+            e_pack_one(A, rec, i);
         }
     }
 }
 
-// H4.ecorrect (hermite.py:96-119)
-__global__ void k_e_correct(EArrays A, const uint64_t *off, const SysCtl *c,
-                            const unsigned *alist, const unsigned *acount)
+// H4.ecorrect (hermite.py:96-119), the records of the corrected state and,
+// after the last pass, the end of the system's step (t += tau).
+__global__ void k_e_correct(EArrays A, const uint64_t *off, SysCtl *c,
+                            float4 *rec, const unsigned *alist,
+                            const unsigned *acount, int last)
 {
-    ACTIVE_LOOP(s, i, alist, acount, off)
+    FOR_ACTIVE_SYSTEM(s, b, e, alist, acount, off)
     {
         const double tau = c[s].tau;
-        for (int d = 0; d < 3; ++d) {
-            const double a0 = A.f0[d][i], a1 = A.f1[d][i];
-            const double j0 = A.f0[3 + d][i], j1 = A.f1[3 + d][i];
-            const double v0 = A.v0[d][i], r0 = A.r0[d][i];
-            const double v1 = (((j0 - j1) * tau / 6 + (a0 + a1)) * tau / 2 + v0);
-            A.v[d][i] = v1;
-            A.r[d][i] = (((a0 - a1) * tau / 6 + (v0 + v1)) * tau / 2 + r0);
+        for (uint64_t i = b + threadIdx.x; i < e; i += blockDim.x) {
+            for (int d = 0; d < 3; ++d) {
+                const double a0 = A.f0[d][i], a1 = A.f1[d][i];
+                const double j0 = A.f0[3 + d][i], j1 = A.f1[3 + d][i];
+                const double v0 = A.v0[d][i], r0 = A.r0[d][i];
+                const double v1 =
+                    (((j0 - j1) * tau / 6 + (a0 + a1)) * tau / 2 + v0);
+                A.v[d][i] = v1;
+                A.r[d][i] = (((a0 - a1) * tau / 6 + (v0 + v1)) * tau / 2 + r0);
+            }
+            e_pack_one(A, rec, i);
         }
-    }
-}
-
-__global__ void k_e_end(SysCtl *c, const int *active, unsigned ns)
-{
-    GRID_LOOP(s, ns)
-    {
-        if (!active[s]) continue;
-        c[s].t += c[s].tau;
-        c[s].nsteps += 1;
+        if (last && threadIdx.x == 0) {
+            c[s].t += tau;
+            c[s].nsteps += 1;
+        }
     }
 }
 
@@ -320,7 +323,6 @@ struct Ensemble {
     unsigned *acount = nullptr;
     uint2 *items = nullptr;         // their i-blocks, same order
     unsigned *icount = nullptr;
-    double **rv_ptrs = nullptr;     // device copies of {r, v}, {r0, v0}
     SysCtl *ctl = nullptr;
     unsigned *queue = nullptr;
     unsigned *err = nullptr;
@@ -340,51 +342,43 @@ unsigned grid_for(uint64_t n, int sms)
     return (unsigned)(b < 1 ? 1 : (b > cap ? cap : b));
 }
 
-// One force evaluation of every active system: pack their records, then
-// one persistent batched sweep over the active list.  which = 0: the
-// current state (r, v); 1: the saved state (r0, v0).
-cudaError_t e_forces(Ensemble *E, int which, double *const *out, int kernel,
-                     double eta)
+// One force evaluation of every active system from the current records:
+// one persistent batched sweep over the (system, i-block) items.
+cudaError_t e_forces(Ensemble *E, double *const *out, int kernel, double eta)
 {
-    double *const *rr = E->rv_ptrs + 6 * which;
-    k_e_pack<<<E->sms * 4, 256, 0, E->stream>>>(E->A, rr, rr + 3, E->pack,
-                                                E->off, E->alist, E->acount);
-    g_launch_count += 1;
-    cudaError_t e = cudaGetLastError();
-    if (e != cudaSuccess) return e;
     return launch_split_batched(kernel, E->pack, E->off, E->alist, E->active,
                                 E->ns, E->queue, (void *const *)out, eta,
                                 E->err, E->sms, E->stream, E->icount,
                                 E->items);
 }
 
+// One Hermite-4 step of every unfinished system (hermite.py:390-410 with
+// epec(2)): nine launches.  The records packed by the kernel that produced
+// the state feed the next sweep, so the step's first two sweeps (Tstep and
+// the forces at the start) share the records left by the previous step.
 cudaError_t e_step(Ensemble *E)
 {
     cudaStream_t st = E->stream;
-    const unsigned gs = grid_for(E->ns, E->sms);
     const unsigned ga = (unsigned)E->sms * 4;   // CTAs over active systems
-    k_e_begin<<<gs, 256, 0, st>>>(E->ctl, E->active, E->ns, E->d_tend,
-                                  E->eta);
-    k_e_compact<<<1, COMPACT_NT, 0, st>>>(E->order, E->active, E->off, E->ns,
-                                          E->alist, E->acount, E->items,
-                                          E->icount);
-    cudaError_t e = e_forces(E, 0, E->A.dt, K_TSTEP, E->eta);
+    k_e_begin<<<1, COMPACT_NT, 0, st>>>(E->ctl, E->active, E->order, E->off,
+                                        E->ns, E->d_tend, E->eta,
+                                        (unsigned)E->sms * 2, E->alist,
+                                        E->acount, E->items, E->icount);
+    cudaError_t e = e_forces(E, E->A.dt, K_TSTEP, E->eta);
     if (e != cudaSuccess) return e;
-    k_e_min<<<ga, 256, 0, st>>>(E->A, E->off, E->ctl, E->alist, E->acount);
-    k_e_block<<<gs, 256, 0, st>>>(E->ctl, E->active, E->ns);
-    k_e_copy<<<ga, 256, 0, st>>>(E->A, E->off, E->alist, E->acount);
-    e = e_forces(E, 1, E->A.f0, K_ACC_JERK, 0.0);
+    k_e_step_size<<<ga, 256, 0, st>>>(E->A, E->off, E->ctl, E->alist,
+                                      E->acount);
+    e = e_forces(E, E->A.f0, K_ACC_JERK, 0.0);
     if (e != cudaSuccess) return e;
-    k_e_predict<<<ga, 256, 0, st>>>(E->A, E->off, E->ctl, E->alist,
+    k_e_predict<<<ga, 256, 0, st>>>(E->A, E->off, E->ctl, E->pack, E->alist,
                                     E->acount);
     for (int pass = 0; pass < 2; ++pass) {
-        e = e_forces(E, 0, E->A.f1, K_ACC_JERK, 0.0);
+        e = e_forces(E, E->A.f1, K_ACC_JERK, 0.0);
         if (e != cudaSuccess) return e;
-        k_e_correct<<<ga, 256, 0, st>>>(E->A, E->off, E->ctl, E->alist,
-                                        E->acount);
+        k_e_correct<<<ga, 256, 0, st>>>(E->A, E->off, E->ctl, E->pack,
+                                        E->alist, E->acount, pass == 1);
     }
-    k_e_end<<<gs, 256, 0, st>>>(E->ctl, E->active, E->ns);
-    g_launch_count += 9;
+    g_launch_count += 5;
     return cudaGetLastError();
 }
 
@@ -458,15 +452,11 @@ TG_EXPORT int tupan_gb300_ensemble_create(unsigned n_sys,
         cudaMalloc((void **)&E->pe, n_sys * sizeof(double)) != cudaSuccess ||
         cudaMalloc((void **)&E->alist, n_sys * sizeof(unsigned)) != cudaSuccess ||
         cudaMalloc((void **)&E->acount, sizeof(unsigned)) != cudaSuccess ||
-        cudaMalloc((void **)&E->items,
-                   (size_t)n_sys * (512 / ITEM_IB) * sizeof(uint2)) != cudaSuccess ||
+        cudaMalloc((void **)&E->items, (size_t)n_sys * 16 * sizeof(uint2)) !=
+            cudaSuccess ||
         cudaMalloc((void **)&E->icount, sizeof(unsigned)) != cudaSuccess ||
-        cudaMalloc((void **)&E->d_tend, sizeof(double)) != cudaSuccess ||
-        cudaMalloc((void **)&E->rv_ptrs, 12 * sizeof(double *)) != cudaSuccess)
+        cudaMalloc((void **)&E->d_tend, sizeof(double)) != cudaSuccess)
         return ST_CUDA;
-    double *rv[12] = {A.r[0],  A.r[1],  A.r[2],  A.v[0],  A.v[1],  A.v[2],
-                      A.r0[0], A.r0[1], A.r0[2], A.v0[0], A.v0[1], A.v0[2]};
-    cudaMemcpy(E->rv_ptrs, rv, sizeof(rv), cudaMemcpyHostToDevice);
     cudaMemset(E->acount, 0, sizeof(unsigned));
     cudaMemset(E->icount, 0, sizeof(unsigned));
     cudaMemcpy(A.sys, sys.data(), n * sizeof(unsigned), cudaMemcpyHostToDevice);
@@ -499,6 +489,10 @@ TG_EXPORT int tupan_gb300_ensemble_evolve(void *handle, double t_end, int batch,
     if (cudaMemcpy(E->d_tend, &t_end, sizeof(double), cudaMemcpyHostToDevice) !=
         cudaSuccess)
         return ST_CUDA;
+    // records of the current state for the first step's sweeps
+    k_e_pack_all<<<(unsigned)E->sms * 8, 256, 0, E->stream>>>(E->A, E->n,
+                                                               E->pack);
+    g_launch_count += 1;
     if (E->graph && E->graph_batch != batch) {
         cudaGraphExecDestroy(E->graph);
         E->graph = nullptr;
@@ -606,7 +600,6 @@ TG_EXPORT int tupan_gb300_ensemble_destroy(void *handle)
     cudaFree(E->items);
     cudaFree(E->icount);
     cudaFree(E->d_tend);
-    cudaFree(E->rv_ptrs);
     cudaFree(E->active);
     cudaFree(E->ctl);
     cudaFree(E->queue);

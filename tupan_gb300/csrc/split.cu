@@ -743,8 +743,8 @@ struct BatchLaunch {
     const int *active;        // per system (may be null: all active)
     unsigned n_sys;
     const unsigned *n_dev;    // if set: item count in device memory
-    const uint2 *items;       // if set: (system, first i) of each item, an
-                              // i-block of at most BATCH_IB particles
+    const uint2 *items;       // if set: (system, ib | ie << 16) of each
+                              // item: the i-block [ib, ie) of the system
     unsigned *queue;          // work counter (zeroed before the launch)
     double *out[MAX_OUT];
     float eta;
@@ -754,13 +754,101 @@ struct BatchLaunch {
 
 constexpr int BATCH_NT = 256;
 constexpr int BATCH_MAXN = 512;           // largest system held in smem
-constexpr int BATCH_IB = 128;             // i-block of an item
+
+// One system's i-range against all of its j: i-data in registers, j-records
+// in shared memory; `lanes` threads share each i (or packed i pair) and
+// split the j loop; FP32 runs of 16 terms folded into Kahan sums.
+template <class Op, bool X2>
+__device__ __forceinline__ void batched_block(const BatchLaunch &L,
+                                              const float4 *rec, uint64_t b,
+                                              int n, int ib, int ni)
+{
+    constexpr int NF = Op::NF, NO = Op::NO, MAXC = Op::MAXC;
+    constexpr int NI = X2 ? 2 : 1;               // i per thread
+    const int tid = threadIdx.x;
+    const int units = (ni + NI - 1) / NI;        // i (pairs) of the block
+    int lanes = 1;
+    while (lanes < 32 && lanes * 2 * units <= BATCH_NT) lanes *= 2;
+    const int groups = BATCH_NT / lanes;
+    const int lane = tid % lanes;
+    for (int u0 = tid / lanes; u0 - tid / lanes < units; u0 += groups) {
+        const int u = u0 < units ? u0 : units - 1;
+        int iv[NI];
+#pragma unroll
+        for (int k = 0; k < NI; ++k) {
+            const int q = u * NI + k;
+            iv[k] = ib + (q < ni ? q : ni - 1);
+        }
+        float sum[NI][NO], corr[NI][NO], part[NI][NO];
+#pragma unroll
+        for (int k = 0; k < NI; ++k)
+#pragma unroll
+            for (int c = 0; c < NO; ++c) sum[k][c] = corr[k][c] = part[k][c] = 0.f;
+        auto fold = [&]() {
+#pragma unroll
+            for (int k = 0; k < NI; ++k)
+#pragma unroll
+                for (int c = 0; c < NO; ++c) {
+                    if (c == MAXC) sum[k][c] = fmaxf(sum[k][c], part[k][c]);
+                    else kahan_add(sum[k][c], corr[k][c], part[k][c]);
+                    part[k][c] = 0.f;
+                }
+        };
+        if constexpr (X2) {
+            using OpX2 = typename X2Of<Op>::type;
+            const typename OpX2::I ip2 = OpX2::pack(
+                Op::load(rec + iv[0] * NF), Op::load(rec + iv[1] * NF));
+            for (int j0 = lane; j0 < n; j0 += 16 * lanes) {
+                float2 p2[NO];
+#pragma unroll
+                for (int c = 0; c < NO; ++c) p2[c] = make_float2(0.f, 0.f);
+                const int je = j0 + 16 * lanes < n ? j0 + 16 * lanes : n;
+                for (int j = j0; j < je; j += lanes)
+                    OpX2::pair(ip2, Op::load(rec + j * NF), p2, L.eta);
+#pragma unroll
+                for (int c = 0; c < NO; ++c) {
+                    part[0][c] = p2[c].x;
+                    part[NI - 1][c] = p2[c].y;
+                }
+                fold();
+            }
+        } else {
+            const typename Op::P ip = Op::load(rec + iv[0] * NF);
+            for (int j0 = lane; j0 < n; j0 += 16 * lanes) {
+                const int je = j0 + 16 * lanes < n ? j0 + 16 * lanes : n;
+                for (int j = j0; j < je; j += lanes)
+                    Op::pair(ip, Op::load(rec + j * NF), part[0], L.eta);
+                fold();
+            }
+        }
+#pragma unroll
+        for (int k = 0; k < NI; ++k) {
+            double v[NO];
+#pragma unroll
+            for (int c = 0; c < NO; ++c) {
+                v[c] = (c == MAXC) ? (double)sum[k][c]
+                                   : (double)sum[k][c] - (double)corr[k][c];
+                for (int o = lanes / 2; o > 0; o >>= 1) {
+                    double w = __shfl_xor_sync(0xffffffffu, v[c], o, lanes);
+                    v[c] = (c == MAXC) ? fmax(v[c], w) : v[c] + w;
+                }
+            }
+            const int q = u0 * NI + k;
+            if (lane == 0 && u0 < units && q < ni) {
+                Op::finish(v, L.eta_d);
+#pragma unroll
+                for (int c = 0; c < NO; ++c) L.out[c][b + iv[k]] = v[c];
+            }
+        }
+    }
+}
 
 template <class Op>
 __global__ void __launch_bounds__(BATCH_NT, 2)
 split_sweep_batched(const BatchLaunch L)
 {
-    constexpr int NF = Op::NF, NO = Op::NO, MAXC = Op::MAXC;
+    constexpr int NF = Op::NF;
+    constexpr bool X2 = !std::is_void<typename X2Of<Op>::type>::value;
     __shared__ __align__(128) float4 rec[BATCH_MAXN * NF];
     __shared__ __align__(8) uint64_t bar;
     __shared__ unsigned item;
@@ -784,66 +872,23 @@ split_sweep_batched(const BatchLaunch L)
         }
         const uint64_t b = L.off[sys];
         const int n = (int)(L.off[sys + 1] - b);
-        // i-range of this item: an i-block, or the whole system
-        const int ib = L.items ? (int)L.items[w].y : 0;
-        const int ie = L.items ? (ib + BATCH_IB < n ? ib + BATCH_IB : n) : n;
-        const int ni = ie - ib;
-        if (n > BATCH_MAXN) {
+        // i-range of this item: an i-block [ib, ie) or the whole system
+        const int ib = L.items ? (int)(L.items[w].y & 0xffffu) : 0;
+        const int ie = L.items ? (int)(L.items[w].y >> 16) : n;
+        if (n > BATCH_MAXN || ie > n || ib >= ie) {
             if (tid == 0) atomicOr(L.err, (unsigned)DERR_BAD_LAUNCH);
             __syncthreads();
             continue;
         }
-        if (tid == 0 && n > 0) {
+        if (tid == 0) {
             const uint32_t bytes = (uint32_t)(n * NF * sizeof(float4));
             mbar_arrive_expect_tx(&bar, bytes);
             bulk_g2s(rec, L.rec + b * NF, bytes, &bar);
         }
-        bool got = n > 0 ? mbar_wait_bounded(&bar, phase, L.err) : true;
-        if (n > 0) phase ^= 1u;
+        bool got = mbar_wait_bounded(&bar, phase, L.err);
+        phase ^= 1u;
         if (!__syncthreads_and(got)) break;
-        // lanes per i: enough to occupy the block, at most 32
-        int lanes = 1;
-        while (lanes < 32 && lanes * 2 * ni <= BATCH_NT) lanes *= 2;
-        const int groups = BATCH_NT / lanes;
-        const int lane = tid % lanes;
-        for (int k0 = tid / lanes; k0 - tid / lanes < ni; k0 += groups) {
-            const int i = ib + (k0 < ni ? k0 : ni - 1);
-            const typename Op::P ip = Op::load(rec + i * NF);
-            float sum[NO], corr[NO], part[NO];
-#pragma unroll
-            for (int c = 0; c < NO; ++c) sum[c] = corr[c] = part[c] = 0.f;
-            int cnt = 0;
-            for (int j = lane; j < n; j += lanes) {
-                const typename Op::P jp = Op::load(rec + j * NF);
-                Op::pair(ip, jp, part, L.eta);
-                if (++cnt == 16) {
-#pragma unroll
-                    for (int c = 0; c < NO; ++c) {
-                        if (c == MAXC) sum[c] = fmaxf(sum[c], part[c]);
-                        else kahan_add(sum[c], corr[c], part[c]);
-                        part[c] = 0.f;
-                    }
-                    cnt = 0;
-                }
-            }
-            double v[NO];
-#pragma unroll
-            for (int c = 0; c < NO; ++c) {
-                if (c == MAXC) sum[c] = fmaxf(sum[c], part[c]);
-                else kahan_add(sum[c], corr[c], part[c]);
-                v[c] = (c == MAXC) ? (double)sum[c]
-                                   : (double)sum[c] - (double)corr[c];
-                for (int o = lanes / 2; o > 0; o >>= 1) {
-                    double u = __shfl_xor_sync(0xffffffffu, v[c], o, lanes);
-                    v[c] = (c == MAXC) ? fmax(v[c], u) : v[c] + u;
-                }
-            }
-            if (lane == 0 && k0 < ni) {
-                Op::finish(v, L.eta_d);
-#pragma unroll
-                for (int c = 0; c < NO; ++c) L.out[c][b + i] = v[c];
-            }
-        }
+        batched_block<Op, X2>(L, rec, b, n, ib, ie - ib);
         __syncthreads();   // the records of this system are no longer read
     }
 }
@@ -871,10 +916,9 @@ cudaError_t launch_split_batched(int kernel, const float4 *rec,
     L.err = err;
     cudaError_t e = cudaMemsetAsync(queue, 0, sizeof(unsigned), st);
     if (e != cudaSuccess) return e;
-    // persistent CTAs; with i-block items a system can occupy up to
-    // BATCH_MAXN / BATCH_IB of them
-    const uint64_t max_items =
-        (uint64_t)n_sys * (items ? BATCH_MAXN / BATCH_IB : 1);
+    // persistent CTAs; with i-block items (at least 32 i each) a system can
+    // occupy up to BATCH_MAXN / 32 of them
+    const uint64_t max_items = (uint64_t)n_sys * (items ? BATCH_MAXN / 32 : 1);
     const unsigned grid =
         (unsigned)((uint64_t)sms * 2 < max_items ? (uint64_t)sms * 2 : max_items);
     if (grid == 0) return cudaSuccess;
