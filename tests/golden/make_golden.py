@@ -271,6 +271,47 @@ def integrators(refroot):
     print("wrote", fn, os.path.getsize(fn))
 
 
+def config1(refroot):
+    """The CPU-runnable configuration in full: Plummer N=256, equal masses,
+    eps=1e-4, tupan's ahermite4 (shared adaptive steps, eta=1/64) to
+    t_end=1, on the reference's own C backend; stores every step size, the
+    final state and the reference's energies at the start and the end
+    (body.py:260-321)."""
+    sys.path.insert(0, refroot)
+    sys.path.insert(0, os.path.dirname(os.path.dirname(HERE)))
+    from tupan.integrator import Integrator
+    from tupan.particles.allparticles import ParticleSystem
+    from tupan_gb300 import ics
+
+    n, eta, t_end = 256, 1.0 / 64, 1.0
+    d = ics.plummer(n, eps=1e-4, seed=256, masses="equal")
+    ps = ParticleSystem(n)
+    ps.mass[...] = d["m"]
+    ps.eps2[...] = d["e2"]
+    for k in ("rx", "ry", "rz", "vx", "vy", "vz"):
+        getattr(ps, k)[...] = d[k]
+    store = {"in/" + k: d[k].copy() for k in
+             ("m", "e2", "rx", "ry", "rz", "vx", "vy", "vz")}
+    store["params"] = np.array([eta, t_end])
+    store["energy0"] = np.array([ps.kinetic_energy, ps.potential_energy])
+    integ = Integrator(eta, 0.0, ps, method="ahermite4")
+    steps = []
+    while abs(integ.time) < t_end:
+        t0 = integ.time
+        integ.evolve_step(t_end)
+        steps.append(integ.time - t0)
+    ps = integ.particle_system
+    store["steps"] = np.array(steps)
+    store["energy1"] = np.array([ps.kinetic_energy, ps.potential_energy])
+    for k in ("rx", "ry", "rz", "vx", "vy", "vz"):
+        store["out/" + k] = np.array(getattr(ps, k), copy=True)
+    e0, e1 = store["energy0"].sum(), store["energy1"].sum()
+    print("config1:", len(steps), "steps, dE/E =", (e1 - e0) / abs(e0))
+    fn = os.path.join(HERE, "golden_config1.npz")
+    np.savez_compressed(fn, **store)
+    print("wrote", fn, os.path.getsize(fn))
+
+
 SIA_RUNS = [
     # (method, n, eps, masses, eta, t_end, max_steps, seed)
     ("sia21h.dkd", 48, 1e-4, "salpeter", 1.0 / 32, 0.25, 6, 31),
@@ -337,7 +378,10 @@ if __name__ == "__main__":
         integrators(ref)
     elif "--sia" in sys.argv:
         sia(ref)
+    elif "--config1" in sys.argv:
+        config1(ref)
     else:
         main(ref)
         integrators(ref)
         sia(ref)
+        config1(ref)

@@ -1,0 +1,54 @@
+"""The CPU-runnable configuration in full on the device-resident Hermite
+driver: Plummer N=256, eps=1e-4, ahermite4 with eta=1/64 to t_end=1 against
+the reference's own run (golden_config1.npz) -- EXACT mode bit for bit over
+all 11747 steps, SPLIT mode within its energy bound."""
+
+import os
+
+import numpy as np
+import pytest
+
+from tupan_gb300.integrator import DeviceHermite
+
+pytestmark = pytest.mark.gpu
+
+GOLDEN = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden",
+                      "golden_config1.npz")
+
+
+def load():
+    z = np.load(GOLDEN)
+    ps = {k: z["in/" + k].copy() for k in
+          ("m", "e2", "rx", "ry", "rz", "vx", "vy", "vz")}
+    eta, t_end = z["params"]
+    return z, ps, float(eta), float(t_end)
+
+
+@pytest.mark.parametrize("batch", [1, 16])
+def test_config1_exact_bit_identical(batch):
+    z, ps, eta, t_end = load()
+    h = DeviceHermite(ps, eta, order=4, adaptive=True, mode="exact",
+                      record_steps=20000)
+    k0, p0 = h.energy()
+    np.testing.assert_allclose([k0, p0], z["energy0"], rtol=1e-13)
+    h.evolve(t_end, batch=batch)
+    np.testing.assert_array_equal(h.steps(), z["steps"])
+    st = h.state()
+    for k in ("rx", "ry", "rz", "vx", "vy", "vz"):
+        np.testing.assert_array_equal(st[k], z["out/" + k], err_msg=k)
+    k1, p1 = h.energy()
+    np.testing.assert_allclose([k1, p1], z["energy1"], rtol=1e-13)
+    h.close()
+
+
+def test_config1_split_energy():
+    z, ps, eta, t_end = load()
+    h = DeviceHermite(ps, eta, order=4, adaptive=True, mode="split")
+    k0, p0 = h.energy()
+    h.evolve(t_end, batch=16)
+    k1, p1 = h.energy()
+    h.close()
+    de = abs(((k1 + p1) - (k0 + p0)) / (k0 + p0))
+    e0, e1 = z["energy0"].sum(), z["energy1"].sum()
+    de_ref = abs((e1 - e0) / e0)
+    assert de <= max(10 * de_ref, 1e-9), (de, de_ref)

@@ -2,6 +2,7 @@
 the EXACT in-order kernel, the queued Kepler path, plain and learned start.
 
     python -m tupan_gb300.sakura_bench --n 4096 --dt 0.001953125 --reps 5
+    python -m tupan_gb300.sakura_bench --integrate --tau 0.00390625 --t-end 0.25
 
 Prints one JSON line: pair evaluations per second of each path, the number
 of Kepler-branch solves per sweep, Kepler solves per second of the queue's
@@ -16,13 +17,62 @@ import os
 import numpy as np
 
 
+def integrate(a):
+    """The Sakura integrator on the device (N = a.n Salpeter Plummer sphere,
+    eps = 0, fixed step tau to t_end), once with the plain Kepler start and
+    once with the learned start: wall time, Kepler solves and their rate,
+    mean Laguerre updates, and the largest difference between the two final
+    states relative to the coordinate scale."""
+    import time
+    import torch
+    from . import ics, learned
+    from .kepler import DeviceSakura
+    ps = ics.plummer(a.n, eps=0.0, seed=11, masses="salpeter")
+    res = {"n": a.n, "tau": a.tau, "t_end": a.t_end}
+    finals = {}
+    net = learned.LearnedStart.load(a.weights or learned.WEIGHTS)
+    for label, use in (("plain", False), ("learned", True)):
+        if use:
+            net.install()
+        d = DeviceSakura(ps)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        t, steps, nk = d.evolve(a.tau, a.t_end, use_mlp=use)
+        wall = time.perf_counter() - t0
+        h = d.hist.copy()
+        finals[label] = d.state()
+        d.close()
+        res[label] = {"steps": int(steps), "wall_s": wall,
+                      "kepler_solves": int(nk),
+                      "kepler_solves_per_s": nk / wall,
+                      "mean_updates": float((np.arange(65) * h).sum() /
+                                            max(h.sum(), 1))}
+    from .kepler import clear_mlp
+    clear_mlp()
+    diff = 0.0
+    for c in ("rx", "ry", "rz", "vx", "vy", "vz"):
+        scale = np.abs(finals["plain"][c]).max()
+        diff = max(diff, float(np.abs(finals["plain"][c] -
+                                      finals["learned"][c]).max() / scale))
+    res["max_state_diff_over_scale"] = diff
+    res["learned_over_plain_wall"] = (res["plain"]["wall_s"] /
+                                      res["learned"]["wall_s"])
+    print(json.dumps(res))
+
+
 def main(argv=None):
     ap = argparse.ArgumentParser()
+    ap.add_argument("--integrate", action="store_true",
+                    help="run the Sakura integrator (plain and learned)")
+    ap.add_argument("--tau", type=float, default=1.0 / 256)
+    ap.add_argument("--t-end", type=float, default=0.25)
     ap.add_argument("--n", type=int, default=4096)
     ap.add_argument("--dt", type=float, default=1.0 / 512)
     ap.add_argument("--reps", type=int, default=5)
     ap.add_argument("--weights", default=None)
     a = ap.parse_args(argv)
+    if a.integrate:
+        return integrate(a)
 
     import torch
     from . import ics, lib, learned
