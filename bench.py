@@ -46,7 +46,9 @@ def parse():
     p.add_argument("--warmup", type=int, default=3)
     p.add_argument("--impl", default="ours", choices=["ours", "reference"])
     p.add_argument("--n", type=int, default=262144)
-    p.add_argument("--fp64-ni", type=int, default=8192)
+    # fp64 EXACT i-subset: two CTAs of 128 i per SM fill the GPU (the cost
+    # is linear in ni; a smaller subset would leave SMs idle)
+    p.add_argument("--fp64-ni", type=int, default=2 * 152 * 128)
     p.add_argument("--cpu-ni", type=int, default=32768)
     p.add_argument("--no-cpu", action="store_true")
     return p.parse_args()
