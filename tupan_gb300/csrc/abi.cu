@@ -57,12 +57,6 @@ int split_variant_count();
 void split_variant_info(int v, int *ni_per_thread, int *jsplit, int *threads);
 bool split_supported(int kernel);
 bool split_has_x2(int kernel);
-bool split_has_dup(int kernel);
-void split_dup_variant_info(int v, int *ni_per_thread, int *jsplit,
-                            int *threads);
-int split_dup_nf_host(int kernel);
-cudaError_t launch_pack_dup(int kernel, uint64_t n, const void *const *attrs,
-                            float4 *out, cudaStream_t st);
 int split_nf_host(int kernel);
 }  // namespace tg
 
@@ -195,33 +189,21 @@ uint64_t tune_key(int kernel, uint64_t ni, uint64_t nj)
 // of "one CTA over all j", i.e. waves x work per CTA, with small penalties
 // for lanes that split j (shuffles, shorter runs) and for the partial-sum
 // pass of grid splits.
-// Variants 7 and 8 read duplicated j-records (launch_pack_dup); only
-// callers that pack j that way (allow_dup) may receive them.
-constexpr int DUP_V0 = 7, DUP_VN = 2;
-
-void variant_info_any(int v, int *nip, int *js, int *nt)
-{
-    if (v >= DUP_V0) split_dup_variant_info(v, nip, js, nt);
-    else split_variant_info(v, nip, js, nt);
-}
-
 void choose_split(const DeviceState *d, int kernel, uint64_t ni, uint64_t nj,
-                  int *variant, int *gsplit, bool allow_dup = true)
+                  int *variant, int *gsplit)
 {
-    if (g_override_variant[kernel] >= 0 &&
-        (allow_dup || g_override_variant[kernel] < DUP_V0)) {
+    if (g_override_variant[kernel] >= 0) {
         *variant = g_override_variant[kernel];
         *gsplit = g_override_gsplit[kernel] > 0 ? g_override_gsplit[kernel] : 1;
         return;
     }
     auto it = g_tuned.find(tune_key(kernel, ni, nj));
-    if (it != g_tuned.end() && (allow_dup || it->second.variant < DUP_V0)) {
+    if (it != g_tuned.end()) {
         *variant = it->second.variant;
         *gsplit = it->second.gsplit;
         return;
     }
-    const bool dup = allow_dup && split_has_dup(kernel);
-    const int nv = dup ? DUP_V0 + DUP_VN : split_variant_count();
+    const int nv = split_variant_count();
     const uint64_t jt = (nj + 255) / 256;
     double best = 1e300;
     *variant = 0;
@@ -229,20 +211,20 @@ void choose_split(const DeviceState *d, int kernel, uint64_t ni, uint64_t nj,
     const bool x2 = split_has_x2(kernel);
     for (int v = 0; v < nv; ++v) {
         int nip, js, nt;
-        variant_info_any(v, &nip, &js, &nt);
+        split_variant_info(v, &nip, &js, &nt);
         // variants 5 and 6 are the packed-pair forms of 0 and (2 i, JS=4)
-        // for phi/acc/acc_jerk/tstep (measured 12-16 % faster on the first
-        // three); snap_crackle would only repeat a scalar variant under
-        // another number.  7 and 8 are 5 and 6 on duplicated j-records.
+        // (measured 12-18 % faster on every SPLIT kernel); 7 and 8 are
+        // packed forms with one CTA per SM, left to measured tuning.
         const bool packed = (v >= 5);
         if (packed && !x2) continue;
+        if (v >= 7) continue;
         const double ipc = (double)(nt / js) * nip;
         const uint64_t gx = (uint64_t)((ni + ipc - 1) / ipc);
         const int per_sm = nt >= 256 ? 2 : 4;
         const double cap = (double)d->sms * per_sm;
         const double eff = (nip == 2 ? 1.0 : 0.9) *
                            (js == 1 ? 1.0 : js <= 4 ? 0.95 : 0.88) *
-                           (packed ? (v >= DUP_V0 ? 1.14 : 1.15) : 1.0);
+                           (packed ? 1.15 : 1.0);
         for (int g = 1; g <= 64; g *= 2) {
             if ((uint64_t)g > jt && g > 1) break;
             const double waves = ceil((double)gx * g / cap);
@@ -284,20 +266,15 @@ int run_device_sweep(DeviceState *d, Sweep &s, cudaStream_t st)
     }();
     int variant, gsplit;
     choose_split(d, k, s.ni, s.nj, &variant, &gsplit);
-    const bool dupj = variant >= DUP_V0;
-    const int njf = dupj ? split_dup_nf_host(k) : nf;
     const size_t ibytes = (size_t)s.ni * nf * sizeof(float4);
-    const size_t jbytes = (same && !dupj) ? 0 : (size_t)s.nj * njf * sizeof(float4);
+    const size_t jbytes = same ? 0 : (size_t)s.nj * nf * sizeof(float4);
     int rc = grow(&d->pack, &d->pack_bytes, ibytes + jbytes + 256, "pack buffer");
     if (rc) return rc;
     float4 *irec = (float4 *)d->pack;
-    float4 *jrec = (same && !dupj) ? irec : (float4 *)((char *)d->pack + ibytes);
+    float4 *jrec = same ? irec : (float4 *)((char *)d->pack + ibytes);
     e = launch_pack(k, s.ni, s.ip, irec, st);
     if (e != cudaSuccess) return cuda_fail(e, "pack launch");
-    if (dupj) {
-        e = launch_pack_dup(k, s.nj, s.jp, jrec, st);
-        if (e != cudaSuccess) return cuda_fail(e, "pack launch");
-    } else if (!same) {
+    if (!same) {
         e = launch_pack(k, s.nj, s.jp, jrec, st);
         if (e != cudaSuccess) return cuda_fail(e, "pack launch");
     }
@@ -456,7 +433,7 @@ void choose_split_public(int kernel, uint64_t ni, uint64_t nj, int *variant,
         *gsplit = 1;
         return;
     }
-    choose_split(d, kernel, ni, nj, variant, gsplit, false);
+    choose_split(d, kernel, ni, nj, variant, gsplit);
 }
 
 int split_nf_host(int k)
@@ -740,7 +717,7 @@ TG_EXPORT int tupan_gb300_set_split_config(int kernel, int variant, int gsplit)
 {
     std::lock_guard<std::mutex> lock(g_mu);
     init_overrides();
-    const int nv = split_has_dup(kernel) ? DUP_V0 + DUP_VN : split_variant_count();
+    const int nv = split_variant_count();
     if (kernel < 0 || kernel >= K_COUNT || variant >= nv)
         return ST_BAD_ARGUMENT;
     g_override_variant[kernel] = variant;
@@ -753,7 +730,7 @@ TG_EXPORT int tupan_gb300_set_tuned(int kernel, uint64_t ni, uint64_t nj,
                                     int variant, int gsplit)
 {
     std::lock_guard<std::mutex> lock(g_mu);
-    const int nv = split_has_dup(kernel) ? DUP_V0 + DUP_VN : split_variant_count();
+    const int nv = split_variant_count();
     if (kernel < 0 || kernel >= K_COUNT || variant < 0 || variant >= nv ||
         gsplit < 1)
         return ST_BAD_ARGUMENT;
@@ -774,14 +751,13 @@ TG_EXPORT int tupan_gb300_split_choice(int kernel, uint64_t ni, uint64_t nj,
     return ST_OK;
 }
 
-// Variants of the SPLIT sweep: 0..6 for every SPLIT kernel, 7 and 8
-// (duplicated j-records) for phi, acc and acc_jerk.
-TG_EXPORT int tupan_gb300_split_variants(void) { return DUP_V0 + DUP_VN; }
+// Variants of the SPLIT sweep (0..8, compiled for every SPLIT kernel).
+TG_EXPORT int tupan_gb300_split_variants(void) { return split_variant_count(); }
 
 TG_EXPORT void tupan_gb300_split_variant_info(int v, int *ni_per_thread,
                                               int *jsplit, int *threads)
 {
-    variant_info_any(v, ni_per_thread, jsplit, threads);
+    split_variant_info(v, ni_per_thread, jsplit, threads);
 }
 
 // One sweep over DEVICE arrays on a caller's stream (NULL: the legacy

@@ -78,60 +78,6 @@ cudaError_t launch_pack(int kernel, uint64_t n, const void *const *attrs,
     return cudaGetLastError();
 }
 
-// j-records for the packed-pair variants 7 and 8: every field duplicated
-// into both lanes of a float2, so the packed operands load straight from
-// shared memory.
-//   acc_jerk (6 float4): {xh xh yh yh} {zh zh xl xl} {yl yl zl zl}
-//                        {vx vx vy vy} {vz vz m m} {e2 e2 0 0}
-//   phi, acc (4 float4): {xh xh yh yh} {zh zh xl xl} {yl yl zl zl} {m m e2 e2}
-__host__ __device__ constexpr int split_dup_nf(int k)
-{
-    return k == K_ACC_JERK ? 6 : 4;
-}
-
-__global__ void pack_dup_records(const PackArgs p, uint64_t n, float4 *out)
-{
-    for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n;
-         i += (uint64_t)gridDim.x * blockDim.x) {
-        float xh, xl, yh, yl, zh, zl;
-        split2(p.a[1][i], xh, xl);
-        split2(p.a[2][i], yh, yl);
-        split2(p.a[3][i], zh, zl);
-        const float m = (float)p.a[0][i], e2 = (float)p.a[4][i];
-        float4 *r = out + i * p.nf;
-        r[0] = make_float4(xh, xh, yh, yh);
-        r[1] = make_float4(zh, zh, xl, xl);
-        r[2] = make_float4(yl, yl, zl, zl);
-        if (p.nf == 6) {
-            const float vx = (float)p.a[5][i], vy = (float)p.a[6][i],
-                        vz = (float)p.a[7][i];
-            r[3] = make_float4(vx, vx, vy, vy);
-            r[4] = make_float4(vz, vz, m, m);
-            r[5] = make_float4(e2, e2, 0.f, 0.f);
-        } else {
-            r[3] = make_float4(m, m, e2, e2);
-        }
-    }
-}
-
-cudaError_t launch_pack_dup(int kernel, uint64_t n, const void *const *attrs,
-                            float4 *out, cudaStream_t st)
-{
-    if (n == 0) return cudaSuccess;
-    if (kernel != K_PHI && kernel != K_ACC && kernel != K_ACC_JERK)
-        return cudaErrorInvalidValue;
-    PackArgs p;
-    p.na = n_attr(kernel);
-    p.nf = split_dup_nf(kernel);
-    for (int a = 0; a < MAX_ATTR; ++a)
-        p.a[a] = a < p.na ? (const double *)attrs[a] : nullptr;
-    uint64_t blocks = (n + 255) / 256;
-    if (blocks > 152 * 16) blocks = 152 * 16;
-    pack_dup_records<<<(unsigned)blocks, 256, 0, st>>>(p, n, out);
-    g_launch_count += 1;
-    return cudaGetLastError();
-}
-
 // ---------------------------------------------------------------------------
 // Two i-particles per thread in packed FP32 (f32x2: .x first i, .y second).
 // One FFMA2/FADD2/FMUL2 does the same operation for both i against the same
@@ -365,94 +311,6 @@ struct SnapS2 {
     }
 };
 
-// Duplicated j-record images (variants 7 and 8).
-struct PosJ2 { float2 xh, yh, zh, xl, yl, zl, m, e2; };
-struct PosVelJ2 { float2 xh, yh, zh, xl, yl, zl, vx, vy, vz, m, e2; };
-
-__device__ __forceinline__ PosJ2 load_pos_j2(const float4 *r)
-{
-    const float4 a = r[0], b = r[1], c = r[2], d = r[3];
-    return {make_float2(a.x, a.y), make_float2(a.z, a.w),
-            make_float2(b.x, b.y), make_float2(b.z, b.w),
-            make_float2(c.x, c.y), make_float2(c.z, c.w),
-            make_float2(d.x, d.y), make_float2(d.z, d.w)};
-}
-
-__device__ __forceinline__ PosVelJ2 load_posvel_j2(const float4 *r)
-{
-    const float4 a = r[0], b = r[1], c = r[2], d = r[3], e = r[4], f = r[5];
-    return {make_float2(a.x, a.y), make_float2(a.z, a.w),
-            make_float2(b.x, b.y), make_float2(b.z, b.w),
-            make_float2(c.x, c.y), make_float2(c.z, c.w),
-            make_float2(d.x, d.y), make_float2(d.z, d.w),
-            make_float2(e.x, e.y), make_float2(e.z, e.w),
-            make_float2(f.x, f.y)};
-}
-
-struct PhiD2 {
-    static constexpr int NFJ = 4;
-    using J = PosJ2;
-    __device__ static J load(const float4 *r) { return load_pos_j2(r); }
-    __device__ static void pair(const PosI2 &i, const J &j, float2 *acc, float)
-    {
-        float2 dx = add2(add2(j.xh, i.nxh), add2(j.xl, i.nxl));
-        float2 dy = add2(add2(j.yh, i.nyh), add2(j.yl, i.nyl));
-        float2 dz = add2(add2(j.zh, i.nzh), add2(j.zl, i.nzl));
-        float2 h2 = add2(i.e2, j.e2);
-        float2 s = fma2(dz, dz, fma2(dy, dy, fma2(dx, dx, h2)));
-        float2 y = rsqrt_nr2(s, h2);
-        acc[0] = fma2(make_float2(-j.m.x, -j.m.y), y, acc[0]);
-    }
-};
-
-struct AccD2 {
-    static constexpr int NFJ = 4;
-    using J = PosJ2;
-    __device__ static J load(const float4 *r) { return load_pos_j2(r); }
-    __device__ static void pair(const PosI2 &i, const J &j, float2 *acc, float)
-    {
-        float2 dx = add2(add2(j.xh, i.nxh), add2(j.xl, i.nxl));
-        float2 dy = add2(add2(j.yh, i.nyh), add2(j.yl, i.nyl));
-        float2 dz = add2(add2(j.zh, i.nzh), add2(j.zl, i.nzl));
-        float2 h2 = add2(i.e2, j.e2);
-        float2 s = fma2(dz, dz, fma2(dy, dy, fma2(dx, dx, h2)));
-        float2 y = rsqrt_nr2(s, h2);
-        float2 mk = mul2(mul2(j.m, y), mul2(y, y));
-        acc[0] = fma2(mk, dx, acc[0]);
-        acc[1] = fma2(mk, dy, acc[1]);
-        acc[2] = fma2(mk, dz, acc[2]);
-    }
-};
-
-struct AccJerkD2 {
-    static constexpr int NFJ = 6;
-    using J = PosVelJ2;
-    __device__ static J load(const float4 *r) { return load_posvel_j2(r); }
-    __device__ static void pair(const PosVelI2 &i, const J &j, float2 *acc,
-                                float)
-    {
-        float2 dx = add2(add2(j.xh, i.nxh), add2(j.xl, i.nxl));
-        float2 dy = add2(add2(j.yh, i.nyh), add2(j.yl, i.nyl));
-        float2 dz = add2(add2(j.zh, i.nzh), add2(j.zl, i.nzl));
-        float2 ux = add2(j.vx, i.nvx);
-        float2 uy = add2(j.vy, i.nvy);
-        float2 uz = add2(j.vz, i.nvz);
-        float2 h2 = add2(i.e2, j.e2);
-        float2 s = fma2(dz, dz, fma2(dy, dy, fma2(dx, dx, h2)));
-        float2 rv = fma2(dz, uz, fma2(dy, uy, mul2(dx, ux)));
-        float2 y = rsqrt_nr2(s, h2);
-        float2 y2 = mul2(y, y);
-        float2 mk = mul2(mul2(j.m, y), y2);
-        float2 nal = mul2(mul2(rv, dup(-3.0f)), y2);
-        acc[0] = fma2(mk, dx, acc[0]);
-        acc[1] = fma2(mk, dy, acc[1]);
-        acc[2] = fma2(mk, dz, acc[2]);
-        acc[3] = fma2(mk, fma2(nal, dx, ux), acc[3]);
-        acc[4] = fma2(mk, fma2(nal, dy, uy), acc[4]);
-        acc[5] = fma2(mk, fma2(nal, dz, uz), acc[5]);
-    }
-};
-
 // Packed-pair partner of each scalar operator (void: none).
 template <class Op> struct X2Of { using type = void; };
 template <> struct X2Of<PhiS> { using type = PhiS2; };
@@ -460,12 +318,6 @@ template <> struct X2Of<AccS> { using type = AccS2; };
 template <> struct X2Of<AccJerkS> { using type = AccJerkS2; };
 template <> struct X2Of<TstepS> { using type = TstepS2; };
 template <> struct X2Of<SnapS> { using type = SnapS2; };
-
-// Duplicated-j partner (variants 7 and 8).
-template <class Op> struct D2Of { using type = void; };
-template <> struct D2Of<PhiS> { using type = PhiD2; };
-template <> struct D2Of<AccS> { using type = AccD2; };
-template <> struct D2Of<AccJerkS> { using type = AccJerkD2; };
 
 // ---------------------------------------------------------------------------
 // The sweep kernel.
@@ -492,24 +344,16 @@ __device__ __forceinline__ void kahan_add(float &sum, float &corr, float x)
     sum = t;
 }
 
-template <class Op, bool DUPJ> struct JRecWidth {
-    static constexpr int value = Op::NF;
-};
-template <class Op> struct JRecWidth<Op, true> {
-    static constexpr int value = D2Of<Op>::type::NFJ;
-};
-
-template <class Op, int NI, int JS, int NT, int MINB, bool X2, bool DUPJ>
+template <class Op, int NI, int JS, int NT, int MINB, bool X2>
 __global__ void __launch_bounds__(NT, MINB)
 split_sweep(const SplitLaunch L)
 {
     using OpX2 = typename X2Of<Op>::type;
-    using OpD2 = typename D2Of<Op>::type;
-    static_assert(!X2 || NI == 2, "packed variant handles two i per thread");
-    static_assert(!DUPJ || X2, "duplicated j-records feed the packed path");
+    static_assert(!X2 || NI % 2 == 0, "packed variants take i in pairs");
+    constexpr int NP = X2 ? NI / 2 : 1;       // packed i pairs per thread
     constexpr int NF = Op::NF, NO = Op::NO, MAXC = Op::MAXC;
-    constexpr int NJF = JRecWidth<Op, DUPJ>::value;   // float4 per j-record
-    constexpr int TJ = (NJF > 5) ? 192 : SPLIT_TILE;
+    constexpr int NJF = NF;                   // float4 per j-record
+    constexpr int TJ = SPLIT_TILE;
     // Records per lane summed in FP32 before a Kahan fold: short runs keep
     // the FP32 rounding of each run small next to the particle's |a|.
     constexpr int FOLD = (TJ / JS) < 16 ? (TJ / JS) : 16;
@@ -582,60 +426,46 @@ split_sweep(const SplitLaunch L)
         const float4 *tile = &ring[t & 1][0];
         const uint64_t j0 = jb + (uint64_t)t * TJ;
         const int n = (int)((je - j0) < (uint64_t)TJ ? (je - j0) : TJ);
-        if constexpr (DUPJ) {
-            // packed path reading duplicated j fields straight from smem
-            const typename OpX2::I ip2 = OpX2::pack(ip[0], ip[1]);
+        if constexpr (X2) {
+            // packed path: the i of this thread in pairs, one float2 per
+            // quantity and pair
+            typename OpX2::I ip2[NP];
+#pragma unroll
+            for (int q = 0; q < NP; ++q)
+                ip2[q] = OpX2::pack(ip[2 * q], ip[2 * q + 1]);
 #pragma unroll 1
             for (int r0 = js; r0 < n; r0 += JS * FOLD) {
-                float2 p2[NO];
+                float2 p2[NP][NO];
 #pragma unroll
-                for (int c = 0; c < NO; ++c) p2[c] = make_float2(0.f, 0.f);
-                if (n == TJ) {
+                for (int q = 0; q < NP; ++q)
 #pragma unroll
-                    for (int u = 0; u < FOLD; ++u)
-                        OpD2::pair(ip2, OpD2::load(tile + (r0 + u * JS) * NJF),
-                                   p2, L.eta);
-                } else {
-#pragma unroll 1
-                    for (int u = 0; u < FOLD && r0 + u * JS < n; ++u)
-                        OpD2::pair(ip2, OpD2::load(tile + (r0 + u * JS) * NJF),
-                                   p2, L.eta);
-                }
-#pragma unroll
-                for (int c = 0; c < NO; ++c) {
-                    part[0][c] = p2[c].x;
-                    part[1 % NI][c] = p2[c].y;
-                }
-                fold();
-            }
-        } else if constexpr (X2) {
-            // packed path: both i of this thread in one float2 per quantity
-            const typename OpX2::I ip2 = OpX2::pack(ip[0], ip[1]);
-#pragma unroll 1
-            for (int r0 = js; r0 < n; r0 += JS * FOLD) {
-                float2 p2[NO];
-#pragma unroll
-                for (int c = 0; c < NO; ++c) p2[c] = make_float2(0.f, 0.f);
+                    for (int c = 0; c < NO; ++c) p2[q][c] = make_float2(0.f, 0.f);
                 if (n == TJ) {
 #pragma unroll
                     for (int u = 0; u < FOLD; ++u) {
                         const typename Op::P jp =
                             Op::load(tile + (r0 + u * JS) * NF);
-                        OpX2::pair(ip2, jp, p2, L.eta);
+#pragma unroll
+                        for (int q = 0; q < NP; ++q)
+                            OpX2::pair(ip2[q], jp, p2[q], L.eta);
                     }
                 } else {
 #pragma unroll 1
                     for (int u = 0; u < FOLD && r0 + u * JS < n; ++u) {
                         const typename Op::P jp =
                             Op::load(tile + (r0 + u * JS) * NF);
-                        OpX2::pair(ip2, jp, p2, L.eta);
+#pragma unroll
+                        for (int q = 0; q < NP; ++q)
+                            OpX2::pair(ip2[q], jp, p2[q], L.eta);
                     }
                 }
 #pragma unroll
-                for (int c = 0; c < NO; ++c) {
-                    part[0][c] = p2[c].x;
-                    part[1 % NI][c] = p2[c].y;
-                }
+                for (int q = 0; q < NP; ++q)
+#pragma unroll
+                    for (int c = 0; c < NO; ++c) {
+                        part[(2 * q) % NI][c] = p2[q][c].x;
+                        part[(2 * q + 1) % NI][c] = p2[q][c].y;
+                    }
                 fold();
             }
         } else if (n == TJ) {
@@ -947,8 +777,10 @@ static const VariantInfo kVariants[] = {
     {1, 4, 256},   // fewer i: lanes share an i and split the j-tile
     {1, 16, 256},
     {1, 32, 128},
-    {2, 1, 256},   // as 0 with packed FP32 pairs (phi, acc, acc_jerk, tstep)
+    {2, 1, 256},   // as 0 with packed FP32 pairs
     {2, 4, 256},   // packed, lanes split the j-tile
+    {4, 1, 256},   // packed, two pairs per thread (one CTA per SM)
+    {2, 1, 256},   // as 5 with the registers of one CTA per SM
 };
 constexpr int N_VARIANTS = sizeof(kVariants) / sizeof(kVariants[0]);
 
@@ -961,7 +793,7 @@ void split_variant_info(int v, int *ni_per_thread, int *jsplit, int *threads)
     *threads = kVariants[v].threads;
 }
 
-// Kernels with a packed-pair (f32x2) operator: variants 5 and 6 use it.
+// Kernels with a packed-pair (f32x2) operator: variants 5 to 8 use it.
 bool split_has_x2(int kernel)
 {
     return kernel == K_PHI || kernel == K_ACC || kernel == K_ACC_JERK ||
@@ -974,15 +806,14 @@ bool split_supported(int kernel)
            kernel == K_TSTEP || kernel == K_SNAP_CRACKLE;
 }
 
-template <class Op, int NI, int JS, int NT, int MINB, bool X2 = false,
-          bool DUPJ = false>
+template <class Op, int NI, int JS, int NT, int MINB, bool X2 = false>
 static cudaError_t run_variant(const SplitLaunch &L, int gsplit,
                                cudaStream_t st)
 {
     constexpr uint64_t IPC = (uint64_t)(NT / JS) * NI;
     const uint64_t gx = (L.ni + IPC - 1) / IPC;
     dim3 grid((unsigned)gx, (unsigned)gsplit);
-    split_sweep<Op, NI, JS, NT, MINB, X2, DUPJ><<<grid, NT, 0, st>>>(L);
+    split_sweep<Op, NI, JS, NT, MINB, X2><<<grid, NT, 0, st>>>(L);
     g_launch_count += 1;
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess || gsplit == 1) return e;
@@ -1014,32 +845,15 @@ static cudaError_t run_op(const SplitLaunch &L, int variant, int gsplit,
         }
     case 7:
     case 8:
-        if constexpr (!std::is_void<typename D2Of<Op>::type>::value) {
-            if (variant == 7)
-                return run_variant<Op, 2, 1, 256, 2, true, true>(L, gsplit, st);
-            return run_variant<Op, 2, 4, 256, 2, true, true>(L, gsplit, st);
+        if constexpr (!std::is_void<typename X2Of<Op>::type>::value) {
+            if (variant == 7) return run_variant<Op, 4, 1, 256, 1, true>(L, gsplit, st);
+            return run_variant<Op, 2, 1, 256, 1, true>(L, gsplit, st);
+        } else {
+            return run_variant<Op, 2, 1, 256, 2>(L, gsplit, st);
         }
-        return cudaErrorInvalidValue;
     default: return cudaErrorInvalidValue;
     }
 }
-
-// Variants 7 and 8 (packed pairs on duplicated j-records, which the caller
-// packs with launch_pack_dup) exist for phi, acc and acc_jerk.
-bool split_has_dup(int kernel)
-{
-    return kernel == K_PHI || kernel == K_ACC || kernel == K_ACC_JERK;
-}
-
-void split_dup_variant_info(int v, int *ni_per_thread, int *jsplit,
-                            int *threads)
-{
-    *ni_per_thread = 2;
-    *jsplit = (v == 8) ? 4 : 1;
-    *threads = 256;
-}
-
-int split_dup_nf_host(int kernel) { return split_dup_nf(kernel); }
 
 // irec/jrec: packed records (launch_pack); out: NO double arrays;
 // partial: gsplit x NO x ni doubles when gsplit > 1.
