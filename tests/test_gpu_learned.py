@@ -46,14 +46,16 @@ def test_training_reduces_loss():
 def test_trained_start_keeps_states_and_cuts_the_iteration_tail():
     """What the trained network (trained on the GPU by
     `python -m tupan_gb300.learned`, shipped as kepler_start.npz) gains over
-    the plain first guess dt/r: converged states are unchanged (same
-    stopping rule), and where the plain guess needs more than two Laguerre
-    updates (larger dt) the mean count and the tail of long solves drop.  At
-    dt = 1/512 both need the minimum of two updates for >99% of pairs."""
+    the plain first guess dt/r when it starts every solve: converged states
+    are unchanged (same stopping rule), and where the plain guess needs more
+    than two Laguerre updates (larger dt) the mean count and the tail of
+    long solves drop.  At dt = 1/512 both need the minimum of two updates
+    for >99% of pairs."""
     pytest.importorskip("torch")
     from tupan_gb300 import kepler as kp
     from tupan_gb300.learned import LearnedStart, evaluate
     net = LearnedStart.load()
+    net.gate = float("-inf")
     net.install()
     try:
         big = evaluate(net, 1.0 / 8, seeds=(77,), n_bodies=2048)
@@ -67,4 +69,33 @@ def test_trained_start_keeps_states_and_cuts_the_iteration_tail():
     tail = lambda h: sum(h[5:])
     assert big["mean_iters_learned"] < big["mean_iters_plain"]
     assert tail(big["hist_learned"]) < 0.5 * tail(big["hist_plain"])
-    assert small["mean_iters_learned"] <= small["mean_iters_plain"] + 0.01
+    # where the plain guess is already at the two-update minimum the network
+    # can only lose a little
+    assert small["mean_iters_learned"] <= small["mean_iters_plain"] + 0.05
+
+
+def test_shipped_gate_uses_the_network_where_it_pays():
+    """The shipped gate (fitted from the measured cost of evaluating the
+    network against the Laguerre updates it saves) keeps the plain guess
+    where that is already at the two-update minimum and uses the network at
+    long steps: no extra updates at dt = 1/512, a halved tail of long
+    solves at dt = 1/8, states unchanged.  (Solve rates: the training
+    report of `python -m tupan_gb300.learned`.)"""
+    pytest.importorskip("torch")
+    from tupan_gb300 import kepler as kp
+    from tupan_gb300.learned import LearnedStart, evaluate
+    net = LearnedStart.load()
+    assert net.gate > float("-inf")
+    net.install()
+    try:
+        rs = [evaluate(net, dt, seeds=(78,), n_bodies=2048)
+              for dt in (1.0 / 512, 1.0 / 8)]
+    finally:
+        kp.clear_mlp()
+    for r in rs:
+        print(r["dt"], r["speedup"], r["mean_iters_plain"],
+              r["mean_iters_learned"])
+        assert r["max_state_diff_rel"] <= 1e-11
+        assert r["mean_iters_learned"] <= r["mean_iters_plain"] + 0.005
+    tail = lambda h: sum(h[5:])
+    assert tail(rs[1]["hist_learned"]) < 0.5 * tail(rs[1]["hist_plain"])

@@ -52,16 +52,38 @@ struct MlpParams {
 
 __device__ __forceinline__ float silu(float x) { return x / (1.0f + __expf(-x)); }
 
-// Features of a single-step solve, from the quantities of kep_setup.
+// Features of a single-step solve, from the quantities of kep_setup, in
+// FP32 (they only feed the network's guess): log r0, log |v0|, the cosine of
+// the angle between r0 and v0, and the orbital phase of the step
+// log(|dt| sqrt(m / r0^3)), formed from logarithms so that no power
+// overflows.  kep_phase alone decides whether the network is evaluated.
+__device__ __forceinline__ float kep_phase(const KepArg<double> &k)
+{
+    const float lr = __logf((float)k.r0);
+    return __logf(fabsf((float)k.dt)) + 0.5f * (__logf((float)k.m) - 3.0f * lr);
+}
+
 __device__ __forceinline__ void kep_features(const KepArg<double> &k,
                                              const double *p, float *f)
 {
-    const double vx = p[3], vy = p[4], vz = p[5];
-    const double v = sqrt(vx * vx + vy * vy + vz * vz);
-    f[0] = (float)log(k.r0);
-    f[1] = (float)log(v > 0 ? v : 1e-300);
-    f[2] = (float)(k.rv0 / (k.r0 * (v > 0 ? v : 1e-300)));
-    f[3] = (float)log(fabs(k.dt) * sqrt(k.m / (k.r0 * k.r0 * k.r0)) + 1e-300);
+    const float vx = (float)p[3], vy = (float)p[4], vz = (float)p[5];
+    const float v = sqrtf(vx * vx + vy * vy + vz * vz);
+    const float vs = v > 0.f ? v : 1e-30f;
+    const float r = (float)k.r0;
+    f[0] = __logf(r);
+    f[1] = __logf(vs);
+    f[2] = (float)k.rv0 / (r * vs);
+    f[3] = kep_phase(k);
+}
+
+// Learned start of one solve: s0 scaled by exp(network); false (keep the
+// plain guess) when the network's output is not finite.
+__device__ __forceinline__ bool learned_start(double s0, double *start,
+                                              float y)
+{
+    if (!isfinite(y)) return false;
+    *start = s0 * (double)__expf(y);
+    return true;
 }
 
 // Weights are shared by every thread of a block: staged once in shared memory
@@ -147,22 +169,22 @@ k_pair_solve(const PairSolve P, unsigned *err)
     KepArg<double> ka;
     double s0;
     const bool moving = kep_setup(P.dt, m, e2, p0, &ka, &s0);
-    if (moving && (P.use_mlp || P.rec_x)) {
+    if (moving && P.use_mlp && !P.rec_x && kep_phase(ka) > P.mlp.gate) {
         float f[MLP_IN];
         kep_features(ka, p0, f);
-        if (P.use_mlp && f[3] > P.mlp.gate) {
-            const float y = mlp_eval(S, f);
-            ctx.use_start = true;
-            ctx.start = s0 * exp((double)y);
-        }
-        if (P.rec_x) {
-            for (int k = 0; k < MLP_IN; ++k) P.rec_x[4 * q + k] = f[k];
-            double root;
-            int it = 0;
-            const int st = kep_laguerre(s0, &root, ka, &it);
-            P.rec_y[q] = (st == 0 && root / s0 > 0)
-                             ? (float)log(root / s0) : __int_as_float(0x7fc00000);
-        }
+        ctx.use_start = learned_start(s0, &ctx.start, mlp_eval(S, f));
+    }
+    if (moving && P.rec_x) {
+        float f[MLP_IN];
+        kep_features(ka, p0, f);
+        if (P.use_mlp && f[3] > P.mlp.gate)
+            ctx.use_start = learned_start(s0, &ctx.start, mlp_eval(S, f));
+        for (int k = 0; k < MLP_IN; ++k) P.rec_x[4 * q + k] = f[k];
+        double root;
+        int it = 0;
+        const int st = kep_laguerre(s0, &root, ka, &it);
+        P.rec_y[q] = (st == 0 && root / s0 > 0)
+                         ? (float)log(root / s0) : __int_as_float(0x7fc00000);
     }
     kep_solve(P.dt, m, e2, p0, p1, ctx);
     for (int c = 0; c < 6; ++c) P.out[6 * q + c] = p1[c];
@@ -315,13 +337,11 @@ k_sakura_kepler(const SakuraArgs A, uint64_t nq, unsigned *err)
     if (A.use_mlp) {
         KepArg<double> ka;
         double s0;
-        if (kep_setup(A.dt, m, e2, pre, &ka, &s0)) {
+        if (kep_setup(A.dt, m, e2, pre, &ka, &s0) &&
+            kep_phase(ka) > A.mlp.gate) {
             float f[MLP_IN];
             kep_features(ka, pre, f);
-            if (f[3] > A.mlp.gate) {
-                ctx.use_start = true;
-                ctx.start = s0 * exp((double)mlp_eval(S, f));
-            }
+            ctx.use_start = learned_start(s0, &ctx.start, mlp_eval(S, f));
         }
     }
     kep_solve(A.dt, m, e2, pre, p1, ctx);

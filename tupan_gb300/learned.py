@@ -186,6 +186,26 @@ class LearnedStart(object):
         kp.set_mlp(self.w1, self._b1, self.w2, self._b2, self.w3, self._b3,
                    self.norm, self.gate)
 
+    def fit_gate(self, X, iters_plain, iters_learned, cost):
+        """Gate on feature 3, log(|dt| sqrt(m/r^3)), that maximises the
+        updates saved net of the network's cost: the start is used where
+        the feature exceeds the gate, and there each solve saves
+        iters_plain - iters_learned updates and pays `cost` update
+        equivalents for evaluating the network.  +inf (never) if no
+        threshold saves anything."""
+        f = np.asarray(X, np.float64)[:, 3]
+        gain = (np.asarray(iters_plain, np.float64)
+                - np.asarray(iters_learned, np.float64) - cost)
+        order = np.argsort(-f, kind="stable")
+        cum = np.cumsum(gain[order])
+        k = int(np.argmax(cum))
+        if cum[k] <= 0:
+            self.gate = float("inf")
+        else:
+            lo = f[order[k + 1]] if k + 1 < len(f) else f[order[k]] - 1.0
+            self.gate = float(0.5 * (f[order[k]] + lo))
+        return self.gate
+
     def set_gate(self, X, iters, excess=0.1):
         """Gate on feature 3, log(|dt| sqrt(m/r^3)): the lowest value above
         which the plain guess averages more than 2 + excess updates."""
@@ -218,11 +238,12 @@ class LearnedStart(object):
 
 
 def training_set(dts=(1.0 / 512,), seeds=range(1, 9), n_bodies=4096,
-                 flags=(-1, 1)):
+                 flags=(-1, 1), keep_pairs=False):
     """(X, Y, iterations) of Kepler-branch pairs solved by the plain solver
-    on the GPU; Y = log(root / plain guess)."""
+    on the GPU; Y = log(root / plain guess).  keep_pairs: also the list of
+    (dt, states, m, e2) batches the samples came from."""
     import torch
-    Xs, Ys, Is = [], [], []
+    Xs, Ys, Is, batches = [], [], [], []
     for dt in dts:
         for seed in seeds:
             for flag in flags:
@@ -238,7 +259,36 @@ def training_set(dts=(1.0 / 512,), seeds=range(1, 9), n_bodies=4096,
                 Xs.append(rx.cpu().numpy())
                 Ys.append(ry.cpu().numpy())
                 Is.append(it.cpu().numpy())
-    return np.concatenate(Xs), np.concatenate(Ys), np.concatenate(Is)
+                if keep_pairs:
+                    batches.append((dt, st, m, e2))
+    out = (np.concatenate(Xs), np.concatenate(Ys), np.concatenate(Is))
+    return out + (batches,) if keep_pairs else out
+
+
+def solve_batches(batches, use_mlp):
+    """Per-pair Laguerre updates and the solve time of every batch, plain or
+    with the installed network."""
+    import torch
+    its, secs, updates = [], 0.0, 0
+    for dt, st, m, e2 in batches:
+        n = len(m)
+        T = lambda a: torch.from_numpy(np.ascontiguousarray(a)).cuda()
+        sm, se, ss = T(m), T(e2), T(st)
+        out = torch.zeros((n, 6), dtype=torch.float64, device="cuda")
+        it = torch.zeros(n, dtype=torch.int32, device="cuda")
+        kp.kepler_pairs(n, dt, sm, se, ss, out, iters=it, use_mlp=use_mlp)
+        torch.cuda.synchronize()
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record()
+        kp.kepler_pairs(n, dt, sm, se, ss, out, iters=it, use_mlp=use_mlp)
+        e1.record()
+        torch.cuda.synchronize()
+        secs += e0.elapsed_time(e1) / 1e3
+        a = it.cpu().numpy()
+        its.append(a)
+        updates += int(a.sum())
+    return np.concatenate(its), secs, updates
 
 
 def evaluate(net, dt, seeds=(101,), n_bodies=4096):
@@ -248,6 +298,7 @@ def evaluate(net, dt, seeds=(101,), n_bodies=4096):
     import torch
     res = {"dt": dt, "pairs": 0}
     its = {"plain": [], "learned": []}
+    secs = {"plain": 0.0, "learned": 0.0}
     worst = 0.0
     for seed in seeds:
         for flag in (-1, 1):
@@ -258,8 +309,16 @@ def evaluate(net, dt, seeds=(101,), n_bodies=4096):
             for key, use in (("plain", False), ("learned", True)):
                 out = torch.zeros((n, 6), dtype=torch.float64, device="cuda")
                 it = torch.zeros(n, dtype=torch.int32, device="cuda")
-                kp.kepler_pairs(n, dt, T(m), T(e2), T(st), out, iters=it,
-                                use_mlp=use)
+                sm, se, ss = T(m), T(e2), T(st)
+                kp.kepler_pairs(n, dt, sm, se, ss, out, iters=it, use_mlp=use)
+                torch.cuda.synchronize()
+                e0 = torch.cuda.Event(enable_timing=True)
+                e1 = torch.cuda.Event(enable_timing=True)
+                e0.record()
+                kp.kepler_pairs(n, dt, sm, se, ss, out, iters=it, use_mlp=use)
+                e1.record()
+                torch.cuda.synchronize()
+                secs[key] += e0.elapsed_time(e1) / 1e3
                 outs[key] = out.cpu().numpy()
                 its[key].append(it.cpu().numpy())
             scale = np.abs(st).max(axis=1)
@@ -272,6 +331,9 @@ def evaluate(net, dt, seeds=(101,), n_bodies=4096):
         res["hist_" + key] = np.bincount(np.minimum(a, 10),
                                          minlength=11).tolist()
     res["max_state_diff_rel"] = worst
+    res["solves_per_s_plain"] = res["pairs"] / secs["plain"]
+    res["solves_per_s_learned"] = res["pairs"] / secs["learned"]
+    res["speedup"] = secs["plain"] / secs["learned"]
     return res
 
 
@@ -287,20 +349,36 @@ def main(argv=None):
     a = ap.parse_args(argv)
     dts = [float(x) for x in a.dts.split(",")]
     t0 = time.time()
-    X, Y, I = training_set(dts=dts, seeds=range(1, a.seeds + 1))
+    X, Y, I, batches = training_set(dts=dts, seeds=range(1, a.seeds + 1),
+                                    keep_pairs=True)
     ok = np.isfinite(Y)
     t1 = time.time()
     net = LearnedStart(seed=0)
     hist = net.fit(X[ok], Y[ok], epochs=a.epochs)
     t2 = time.time()
-    net.set_gate(X[ok], I[ok])
+    # gate from measured costs: the network on every solve against the
+    # plain start, on the training pairs
+    net.gate = float("-inf")
+    net.install()
+    it_l, t_l, u_l = solve_batches(batches, True)
+    kp.clear_mlp()
+    it_p, t_p, u_p = solve_batches(batches, False)
+    per_update = t_p / max(u_p, 1)
+    cost = max(0.0, (t_l - per_update * u_l) / per_update / len(it_l))
+    net.fit_gate(X, it_p, it_l, cost)
     net.save(a.out)
     net.install()
     evals = [evaluate(net, dt) for dt in dts]
+    gate = net.gate
+    net.gate = float("-inf")          # the network on every solve
+    net.install()
+    evals_all = [evaluate(net, dt) for dt in dts]
+    net.gate = gate
     kp.clear_mlp()
     print(json.dumps({"samples": int(ok.sum()), "data_s": t1 - t0,
-                      "train_s": t2 - t1, "gate": net.gate, "loss": hist,
-                      "eval": evals}))
+                      "train_s": t2 - t1, "gate": net.gate,
+                      "network_cost_updates": cost, "loss": hist,
+                      "eval": evals, "eval_everywhere": evals_all}))
 
 
 if __name__ == "__main__":
