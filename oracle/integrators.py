@@ -13,6 +13,10 @@ the reference's C backend:
 * ``sakura_step``   tupan/integrator/sakura.py:22-50, :100-117 (asakura step)
 * ``evolve``        tupan/simulation.py:187-198 loop over evolve_step
                     (tupan/integrator/__init__.py:80-99)
+* ``nreg_evolve``   tupan/integrator/nreg.py:22-170 (nreg_x, nreg_v,
+                    anreg_step, nreg_step, NREG.initialize and do_step)
+* ``pairwise_sum``  numpy's summation order for float64 arrays (the
+                    reference's .sum() calls), restated for the device
 
 A state is a dict of float64 arrays m, rx, ry, rz, e2, vx, vy, vz.
 """
@@ -319,3 +323,109 @@ def block_step(st, order, eta, dt_max):
     st["dt"][act] = [block_tstep(abs(x), t_next, dt_max) for x in dt_a]
     st["t"][act] = t_next
     return t_next, len(act)
+
+
+# ---------------------------------------------------------------------------
+# NREG (tupan/integrator/nreg.py): the regularised time transform with
+# scalar W, U, S carried between the position and velocity updates.
+# ---------------------------------------------------------------------------
+def pairwise_sum(a, lo=0, n=None):
+    """numpy's add.reduce order for a contiguous float64 array: below 8
+    elements a sequential sum from 0.0; up to 128 elements eight running
+    sums over strided elements, combined as ((r0+r1)+(r2+r3))+((r4+r5)+
+    (r6+r7)), then the tail; above that the two halves (the first rounded
+    down to a multiple of 8) summed recursively and added."""
+    if n is None:
+        n = len(a)
+    if n < 8:
+        res = 0.0
+        for i in range(n):
+            res += a[lo + i]
+        return res
+    if n <= 128:
+        r = [a[lo + j] for j in range(8)]
+        i = 8
+        while i < n - (n % 8):
+            for j in range(8):
+                r[j] += a[lo + i + j]
+            i += 8
+        res = ((r[0] + r[1]) + (r[2] + r[3])) + ((r[4] + r[5]) + (r[6] + r[7]))
+        while i < n:
+            res += a[lo + i]
+            i += 1
+        return res
+    n2 = n // 2
+    n2 -= n2 % 8
+    return pairwise_sum(a, lo, n2) + pairwise_sum(a, lo + n2, n - n2)
+
+
+class NregState(object):
+    """ParticleSystem class attributes the reference keeps for NREG."""
+
+    def __init__(self, ps):
+        self.t = 0.0
+        mtot = float(ps["m"].sum())
+        k, p = energies(ps)
+        self.E0 = k + p
+        self.W = -p
+        self.U = -p
+        self.S = -p
+        self.mtot = mtot
+
+
+def nreg_x(ps, st, dt):
+    """nreg.py:22-34"""
+    out = _kern("nreg_Xkernel", ps, None, {"dt": dt})
+    for k, v in zip(("mrx", "mry", "mrz", "ax", "ay", "az", "u"), out):
+        ps[k] = v
+    mtot = float(ps["m"].sum())
+    for c in "xyz":
+        ps["r" + c] = ps["mr" + c] / mtot
+    st.U = 0.5 * ps["u"].sum()
+    st.t += dt
+
+
+def nreg_v(ps, st, dt):
+    """nreg.py:46-57"""
+    out = _kern("nreg_Vkernel", ps, None, {"dt": dt})
+    for k, v in zip(("mvx", "mvy", "mvz", "mk"), out):
+        ps[k] = v
+    mtot = float(ps["m"].sum())
+    for c in "xyz":
+        ps["v" + c] = ps["mv" + c] / mtot
+    K = 0.25 * ps["mk"].sum() / mtot
+    st.W = (K - st.E0)
+
+
+def anreg_step(ps, st, h):
+    """nreg.py:77-86"""
+    nreg_x(ps, st, 0.5 * (h / st.W))
+    nreg_v(ps, st, (h / st.U))
+    nreg_x(ps, st, 0.5 * (h / st.W))
+
+
+def nreg_step(ps, st, h):
+    """nreg.py:89-98"""
+    anreg_step(ps, st, 0.5 * (h * st.S))
+    st.S = 1 / (2 / st.W - 1 / st.S)
+    anreg_step(ps, st, 0.5 * (h * st.S))
+
+
+def nreg_evolve(ps, t_end, eta, method, max_steps=None):
+    """NREG.initialize + the evolve loop over NREG.do_step (nreg.py:111-
+    170).  Returns (state scalars, list of t after each step); ps (a dict
+    with ax, ay, az zero-initialised if absent) is advanced in place."""
+    for k in ("ax", "ay", "az"):
+        ps.setdefault(k, np.zeros(len(ps["m"])))
+    st = NregState(ps)
+    times = []
+    while abs(st.t) < t_end:
+        tau = base_tstep(st.t, t_end, eta)
+        if "anreg" in method:
+            anreg_step(ps, st, tau / 2)
+        else:
+            nreg_step(ps, st, tau)
+        times.append(st.t)
+        if max_steps is not None and len(times) >= max_steps:
+            break
+    return st, times

@@ -312,6 +312,56 @@ def config1(refroot):
     print("wrote", fn, os.path.getsize(fn))
 
 
+NREG_RUNS = [
+    # (method, n, eps, masses, eta, t_end, max_steps, seed)
+    ("nreg", 64, 1e-2, "equal", 1.0 / 64, 0.25, 12, 51),
+    ("anreg", 64, 1e-2, "equal", 1.0 / 64, 0.25, 12, 52),
+    ("nreg", 40, 1e-3, "salpeter", 1.0 / 128, 0.25, 10, 53),
+    ("anreg", 200, 1e-3, "salpeter", 1.0 / 128, 0.25, 6, 54),
+]
+
+
+def nreg(refroot):
+    """Short runs of the reference's NREG integrators (tupan/integrator/
+    nreg.py) on its C backend: the time after each step, the final state
+    and the final W, U, S (class attributes of the particle system)."""
+    sys.path.insert(0, refroot)
+    sys.path.insert(0, os.path.dirname(os.path.dirname(HERE)))
+    from tupan.integrator import Integrator
+    from tupan.particles.allparticles import ParticleSystem
+    from tupan_gb300 import ics
+
+    store = {}
+    for r, (method, n, eps, masses, eta, t_end, max_steps, seed) in \
+            enumerate(NREG_RUNS):
+        d = ics.plummer(n, eps=eps, seed=seed, masses=masses)
+        ps = ParticleSystem(n)
+        ps.mass[...] = d["m"]
+        ps.eps2[...] = d["e2"]
+        for k in ("rx", "ry", "rz", "vx", "vy", "vz"):
+            getattr(ps, k)[...] = d[k]
+        tag = "%d/" % r
+        store[tag + "method"] = np.array(method)
+        for k in ("m", "e2", "rx", "ry", "rz", "vx", "vy", "vz"):
+            store[tag + "in/" + k] = d[k].copy()
+        integ = Integrator(eta, 0.0, ps, method=method)
+        times = []
+        while abs(integ.time) < t_end and len(times) < max_steps:
+            integ.evolve_step(t_end)
+            times.append(integ.time)
+        ps = integ.particle_system
+        store[tag + "times"] = np.array(times)
+        store[tag + "params"] = np.array([eta, t_end, max_steps])
+        store[tag + "scalars"] = np.array([type(ps).W, type(ps).U,
+                                           type(ps).S, type(ps).E0])
+        for k in ("rx", "ry", "rz", "vx", "vy", "vz"):
+            store[tag + "out/" + k] = np.array(getattr(ps, k), copy=True)
+        print(method, n, len(times), "steps, t =", integ.time)
+    fn = os.path.join(HERE, "golden_nreg.npz")
+    np.savez_compressed(fn, **store)
+    print("wrote", fn, os.path.getsize(fn))
+
+
 SIA_RUNS = [
     # (method, n, eps, masses, eta, t_end, max_steps, seed)
     ("sia21h.dkd", 48, 1e-4, "salpeter", 1.0 / 32, 0.25, 6, 31),
@@ -380,8 +430,11 @@ if __name__ == "__main__":
         sia(ref)
     elif "--config1" in sys.argv:
         config1(ref)
+    elif "--nreg" in sys.argv:
+        nreg(ref)
     else:
         main(ref)
         integrators(ref)
         sia(ref)
         config1(ref)
+        nreg(ref)
