@@ -433,6 +433,31 @@ int tupan_gb300_sia_stats(void *handle, long long *stats);
 int tupan_gb300_sia_set_subtree(void *handle, int max_n);
 int tupan_gb300_sia_destroy(void *handle);
 
+/* ------------------------------------------------------------------------
+ * NREG integrators (libtupan_gb300.so only).  No counterpart in the
+ * reference's C ABI: tupan/integrator/nreg.py runs the regularised-time
+ * recurrences on host arrays around the nreg_X / nreg_V kernels.  Here the
+ * particles stay in HBM; sums are taken in numpy's pairwise order, so a run
+ * is bit-identical to the reference's.
+ * ---------------------------------------------------------------------- */
+/* anreg 0: "nreg", 1: "anreg".  Host arrays are copied in. */
+int tupan_gb300_nreg_create(uint64_t n, int anreg, double eta,
+                            const double *m, const double *e2,
+                            const double *rx, const double *ry,
+                            const double *rz, const double *vx,
+                            const double *vy, const double *vz,
+                            void **handle);
+/* Steps until |t| >= t_end or max_steps (0: no limit); t_log (host, may be
+ * NULL) receives the time after each step (at most log_cap). */
+int tupan_gb300_nreg_evolve(void *handle, double t_end, long long max_steps,
+                            double *t_out, long long *steps_out,
+                            double *t_log, long long log_cap);
+/* State (host arrays of n, may be NULL) and scalars[5] = {W, U, S, E0, t}. */
+int tupan_gb300_nreg_get_state(void *handle, double *rx, double *ry,
+                               double *rz, double *vx, double *vy,
+                               double *vz, double *scalars);
+int tupan_gb300_nreg_destroy(void *handle);
+
 #ifdef __cplusplus
 }
 #endif

@@ -39,7 +39,7 @@ def float64_only():
     prefixes = ("tupan_gb300_hermite_", "tupan_gb300_block_",
                 "tupan_gb300_sakura_", "tupan_gb300_kepler_",
                 "tupan_gb300_mlp_", "tupan_gb300_ensemble_",
-                "tupan_gb300_sia_")
+                "tupan_gb300_sia_", "tupan_gb300_nreg_")
     return {n for n in header_functions()
             if n.startswith(prefixes) or n.endswith("_noalloc")}
 

@@ -38,11 +38,12 @@ UNITS = {
     "ensemble.o": ("ensemble.cu", ["-fmad=false"]),
     "noalloc.o": ("noalloc.cu", []),
     "sia.o": ("sia.cu", ["-fmad=false"]),
+    "nreg.o": ("nreg.cu", ["-fmad=false"]),
 }
 LINKS = {
     LIB64: ["exact.o", "split.o", "abi64.o", "microbench.o", "driver.o",
             "blockstep.o", "sakura.o", "mlp.o", "ensemble.o",
-            "noalloc.o", "sia.o"],
+            "noalloc.o", "sia.o", "nreg.o"],
     LIB32: ["exact.o", "split.o", "abi32.o", "microbench.o"],
 }
 

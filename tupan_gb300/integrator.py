@@ -294,3 +294,77 @@ class DeviceSIA(object):
             self.close()
         except Exception:
             pass
+
+
+def _declare_nreg(L):
+    c = ctypes
+    L.tupan_gb300_nreg_create.argtypes = (
+        [c.c_uint64, c.c_int, c.c_double] + [_DP] * 8
+        + [c.POINTER(c.c_void_p)])
+    L.tupan_gb300_nreg_create.restype = c.c_int
+    L.tupan_gb300_nreg_evolve.argtypes = [
+        c.c_void_p, c.c_double, c.c_longlong, _DP, c.POINTER(c.c_longlong),
+        _DP, c.c_longlong]
+    L.tupan_gb300_nreg_evolve.restype = c.c_int
+    L.tupan_gb300_nreg_get_state.argtypes = [c.c_void_p] + [_DP] * 7
+    L.tupan_gb300_nreg_get_state.restype = c.c_int
+    L.tupan_gb300_nreg_destroy.argtypes = [c.c_void_p]
+    L.tupan_gb300_nreg_destroy.restype = c.c_int
+
+
+class DeviceNreg(object):
+    """tupan's regularised-time integrators ``nreg`` and ``anreg``
+    (tupan/integrator/nreg.py) with the particles in HBM; see csrc/nreg.cu.
+    EXACT sweeps and numpy's summation order: bit-identical to the
+    reference's runs."""
+
+    def __init__(self, ps, method, eta):
+        if method not in ("nreg", "anreg"):
+            raise ValueError("unexpected NREG method: %r" % (method,))
+        self.L = lib.load("float64")
+        _declare_nreg(self.L)
+        self.n = len(ps["m"])
+        arrs = [np.ascontiguousarray(ps[k], dtype=np.float64)
+                for k in ("m", "e2", "rx", "ry", "rz", "vx", "vy", "vz")]
+        h = ctypes.c_void_p()
+        st = self.L.tupan_gb300_nreg_create(
+            self.n, 1 if method == "anreg" else 0, float(eta),
+            *[_p(a) for a in arrs], ctypes.byref(h))
+        if st:
+            raise lib.TupanGB300Error("nreg_create failed: status %d" % st)
+        self.h = h
+
+    def evolve(self, t_end, max_steps=0):
+        cap = int(max_steps) if max_steps else 1 << 16
+        log = np.zeros(cap)
+        t = ctypes.c_double()
+        k = ctypes.c_longlong()
+        st = self.L.tupan_gb300_nreg_evolve(self.h, float(t_end),
+                                            int(max_steps), ctypes.byref(t),
+                                            ctypes.byref(k), _p(log), cap)
+        if st:
+            raise lib.TupanGB300Error("nreg_evolve failed: status %d" % st)
+        return log[:min(k.value, cap)].copy()
+
+    def state(self):
+        out = {k: np.empty(self.n) for k in
+               ("rx", "ry", "rz", "vx", "vy", "vz")}
+        sc = np.zeros(5)
+        st = self.L.tupan_gb300_nreg_get_state(
+            self.h, *[_p(out[k]) for k in ("rx", "ry", "rz", "vx", "vy",
+                                           "vz")], _p(sc))
+        if st:
+            raise lib.TupanGB300Error("nreg_get_state failed")
+        out.update(zip(("W", "U", "S", "E0", "t"), (float(x) for x in sc)))
+        return out
+
+    def close(self):
+        if self.h:
+            self.L.tupan_gb300_nreg_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
