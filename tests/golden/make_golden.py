@@ -362,6 +362,37 @@ def nreg(refroot):
     print("wrote", fn, os.path.getsize(fn))
 
 
+PLUMMER_RUNS = [
+    # (n, eps, imf, seed, softening_type)
+    (256, 1e-4, ("equalmass",), 1, 0),
+    (1000, 1e-3, ("salpeter1955", 0.5, 10.0), 2, 0),
+    (500, 1e-2, ("equalmass",), 3, 2),
+    (300, 1e-3, ("parravano2011", 0.1, 20.0), 4, 1),
+]
+
+
+def plummer(refroot):
+    """The reference's own initial conditions (tupan/ics/plummer.py:213-221
+    make_plummer) for a few sizes, IMFs and softening types."""
+    sys.path.insert(0, refroot)
+    from tupan.ics.plummer import make_plummer
+
+    store = {}
+    for r, (n, eps, imf, seed, stype) in enumerate(PLUMMER_RUNS):
+        ps = make_plummer(n, eps, imf, seed=seed, softening_type=stype)
+        tag = "%d/" % r
+        store[tag + "params"] = np.array([n, eps, seed, stype])
+        store[tag + "imf"] = np.array([str(x) for x in imf])
+        for k, a in (("m", "mass"), ("e2", "eps2"), ("rx", "rx"),
+                     ("ry", "ry"), ("rz", "rz"), ("vx", "vx"), ("vy", "vy"),
+                     ("vz", "vz"), ("phi", "phi")):
+            store[tag + k] = np.array(getattr(ps, a), copy=True)
+        print("plummer", n, imf, "m sum", ps.mass.sum())
+    fn = os.path.join(HERE, "golden_plummer_ics.npz")
+    np.savez_compressed(fn, **store)
+    print("wrote", fn, os.path.getsize(fn))
+
+
 SIA_RUNS = [
     # (method, n, eps, masses, eta, t_end, max_steps, seed)
     ("sia21h.dkd", 48, 1e-4, "salpeter", 1.0 / 32, 0.25, 6, 31),
@@ -432,9 +463,12 @@ if __name__ == "__main__":
         config1(ref)
     elif "--nreg" in sys.argv:
         nreg(ref)
+    elif "--plummer" in sys.argv:
+        plummer(ref)
     else:
         main(ref)
         integrators(ref)
         sia(ref)
         config1(ref)
         nreg(ref)
+        plummer(ref)

@@ -481,9 +481,13 @@ TG_EXPORT int tupan_gb300_block_evolve(void *handle, double t_end,
     if (!b) return ST_BAD_ARGUMENT;
     long long k = 0;
     while (b->t < t_end && (max_steps <= 0 || k < max_steps)) {
+        const double t_before = b->t;
         int rc = b->order == 4 ? block_step<4>(b)
                : b->order == 6 ? block_step<6>(b) : block_step<8>(b);
         if (rc) return rc;
+        // the block time must advance (a zero or non-finite step would
+        // loop forever)
+        if (!(b->t > t_before)) return ST_DEVICE;
         ++k;
     }
     if (cudaStreamSynchronize(b->stream) != cudaSuccess) return ST_CUDA;

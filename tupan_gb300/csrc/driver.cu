@@ -498,11 +498,16 @@ TG_EXPORT int tupan_gb300_hermite_evolve(void *handle, double t_end,
     }
     StepCtl c;
     long long start = -1;
+    double t_prev = NAN;
     for (;;) {
         cudaMemcpy(&c, h->ctl, sizeof(c), cudaMemcpyDeviceToHost);
         if (start < 0) start = c.nsteps;
         if (fabs(c.t) >= t_end || (max_steps > 0 && c.nsteps - start >= max_steps))
             break;
+        // a step that does not advance time (a zero or non-finite step
+        // size) would loop forever: report it instead
+        if (!isfinite(c.t) || c.t == t_prev) return ST_DEVICE;
+        t_prev = c.t;
         long long left = max_steps > 0 ? max_steps - (c.nsteps - start) : batch;
         if (left < batch) {
             // finish with single uncaptured steps so max_steps is exact
