@@ -372,6 +372,8 @@ int block_step(Block *b)
 
 // Creates a system from HOST arrays and initialises forces and steps at t=0.
 // order 4, 6 or 8; mode 0 EXACT / 1 SPLIT; dt_max caps every step.
+TG_EXPORT int tupan_gb300_block_destroy(void *handle);
+
 TG_EXPORT int tupan_gb300_block_create(uint64_t n, int order, int mode,
                                        double eta, double dt_max,
                                        const double *m, const double *e2,
@@ -384,6 +386,7 @@ TG_EXPORT int tupan_gb300_block_create(uint64_t n, int order, int mode,
         (order != 4 && order != 6 && order != 8) || !(dt_max > 0))
         return ST_BAD_ARGUMENT;
     Block *b = new Block();
+    CreateGuard guard{b, tupan_gb300_block_destroy};
     b->n = n;
     b->order = order;
     b->mode = mode == MODE_SPLIT ? MODE_SPLIT : MODE_EXACT;
@@ -466,6 +469,7 @@ TG_EXPORT int tupan_gb300_block_create(uint64_t n, int order, int mode,
     g_launch_count += 1;
     if (cudaStreamSynchronize(b->stream) != cudaSuccess) return ST_CUDA;
     *handle = b;
+    guard.keep();
     return ST_OK;
 }
 
@@ -528,7 +532,7 @@ TG_EXPORT int tupan_gb300_block_destroy(void *handle)
     cudaFree(b->pack_i);
     cudaFree(b->pack_j);
     cudaFree(b->partial);
-    cudaStreamDestroy(b->stream);
+    if (b->stream) cudaStreamDestroy(b->stream);
     delete b;
     return ST_OK;
 }

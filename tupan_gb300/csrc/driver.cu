@@ -393,6 +393,8 @@ cudaError_t one_step(Hermite *h)
 // adaptive: 1 = tupan's "ahermiteN" (Tstep + power-of-two quantisation),
 // 0 = "hermiteN" (step = eta); mode: 0 EXACT, 1 SPLIT forces.  tau_log_cap:
 // number of step sizes to record (0: none).
+TG_EXPORT int tupan_gb300_hermite_destroy(void *handle);
+
 TG_EXPORT int tupan_gb300_hermite_create(
     uint64_t n, int order, int adaptive, int mode, double eta,
     const double *m, const double *e2, const double *rx, const double *ry,
@@ -403,6 +405,7 @@ TG_EXPORT int tupan_gb300_hermite_create(
                               order != 8))
         return ST_BAD_ARGUMENT;
     Hermite *h = new Hermite();
+    CreateGuard guard{h, tupan_gb300_hermite_destroy};
     h->n = n;
     h->order = order;
     h->adaptive = adaptive ? 1 : 0;
@@ -460,6 +463,7 @@ TG_EXPORT int tupan_gb300_hermite_create(
     choose_split_public(K_ACC_JERK, n, n, &v, &gs);   // initialise device state
     if (cudaDeviceSynchronize() != cudaSuccess) return ST_CUDA;
     *handle = h;
+    guard.keep();
     return ST_OK;
 }
 
@@ -606,7 +610,7 @@ TG_EXPORT int tupan_gb300_hermite_destroy(void *handle)
     cudaFree(h->partial);
     cudaFree(h->epart);
     cudaFree(h->v3);
-    cudaStreamDestroy(h->stream);
+    if (h->stream) cudaStreamDestroy(h->stream);
     delete h;
     return ST_OK;
 }

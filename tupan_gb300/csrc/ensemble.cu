@@ -390,6 +390,8 @@ cudaError_t e_step(Ensemble *E)
 
 // n_sys systems; sys_off[n_sys + 1] host offsets into the concatenated HOST
 // arrays m, e2, r, v (sizes 1 .. 512 each).  Forces are SPLIT-mode.
+TG_EXPORT int tupan_gb300_ensemble_destroy(void *handle);
+
 TG_EXPORT int tupan_gb300_ensemble_create(unsigned n_sys,
                                           const uint64_t *sys_off, double eta,
                                           const double *m, const double *e2,
@@ -404,6 +406,7 @@ TG_EXPORT int tupan_gb300_ensemble_create(unsigned n_sys,
         if (sys_off[s + 1] < sys_off[s] || sys_off[s + 1] - sys_off[s] > 512)
             return ST_TOO_LARGE;
     Ensemble *E = new Ensemble();
+    CreateGuard guard{E, tupan_gb300_ensemble_destroy};
     E->n = n;
     E->ns = n_sys;
     E->eta = eta;
@@ -474,6 +477,7 @@ TG_EXPORT int tupan_gb300_ensemble_create(unsigned n_sys,
             return ST_CUDA;
     if (cudaDeviceSynchronize() != cudaSuccess) return ST_CUDA;
     *handle = E;
+    guard.keep();
     return ST_OK;
 }
 
@@ -607,7 +611,7 @@ TG_EXPORT int tupan_gb300_ensemble_destroy(void *handle)
     cudaFree(E->pack);
     cudaFree(E->ke);
     cudaFree(E->pe);
-    cudaStreamDestroy(E->stream);
+    if (E->stream) cudaStreamDestroy(E->stream);
     delete E;
     return ST_OK;
 }

@@ -614,6 +614,8 @@ struct SakuraSys {
 
 }  // namespace
 
+TG_EXPORT int tupan_gb300_sakura_destroy(void *handle);
+
 TG_EXPORT int tupan_gb300_sakura_create(uint64_t n, const double *m,
                                         const double *e2, const double *rx,
                                         const double *ry, const double *rz,
@@ -622,6 +624,7 @@ TG_EXPORT int tupan_gb300_sakura_create(uint64_t n, const double *m,
 {
     if (!handle || n == 0) return ST_BAD_ARGUMENT;
     SakuraSys *S = new SakuraSys();
+    CreateGuard guard{S, tupan_gb300_sakura_destroy};
     S->n = n;
     if (cudaStreamCreateWithFlags(&S->stream, cudaStreamNonBlocking) !=
             cudaSuccess ||
@@ -640,6 +643,7 @@ TG_EXPORT int tupan_gb300_sakura_create(uint64_t n, const double *m,
     cudaMemcpy(S->xd, xs, sizeof(xs), cudaMemcpyHostToDevice);
     cudaMemcpy(S->dd, S->d, sizeof(S->d), cudaMemcpyHostToDevice);
     *handle = S;
+    guard.keep();
     return ST_OK;
 }
 
@@ -713,7 +717,7 @@ TG_EXPORT int tupan_gb300_sakura_destroy(void *handle)
     cudaFree(S->pool);
     cudaFree(S->xd);
     cudaFree(S->dd);
-    cudaStreamDestroy(S->stream);
+    if (S->stream) cudaStreamDestroy(S->stream);
     delete S;
     return ST_OK;
 }

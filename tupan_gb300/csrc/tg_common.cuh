@@ -107,6 +107,19 @@ struct Workspace {
     unsigned *err;       // device error word
 };
 
+// Frees a half-built object when a create entry point fails part way:
+// construct right after `new`, call keep() once the object is complete.
+struct CreateGuard {
+    void *obj;
+    int (*destroy)(void *);
+    bool kept = false;
+    void keep() { kept = true; }
+    ~CreateGuard()
+    {
+        if (!kept && obj) destroy(obj);
+    }
+};
+
 }  // namespace tg
 
 #define TG_CUDA_TRY(expr)                                                   \
