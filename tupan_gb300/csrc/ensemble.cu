@@ -3,19 +3,18 @@
 // (tupan's "ahermite4": hermite.py:390-410 with the quantisation of
 // integrator/__init__.py:59-78), each system's step held in device memory.
 //
-// Every force evaluation of the whole ensemble is ONE launch of the batched
-// SPLIT sweep (split_sweep_batched: a persistent kernel whose CTAs take
-// systems from an atomic work queue, largest first); the per-particle
-// predictor/corrector and the per-system step control are elementwise
-// kernels.  A step is a fixed sequence of nine launches, so `batch` steps
-// are captured in a CUDA graph and replayed.  Each step first compacts the
-// systems that have not reached t_end into a list (largest first) and
-// splits them into (system, i-block) work items; the sweeps and the
-// per-system kernels walk only that list, and the kernel that produces a
-// state also packs the FP32 records the next sweep reads.  A run is
-// usually dominated by a few systems with hard binaries that need
+// Every force evaluation of the whole ensemble is ONE launch of a
+// persistent batched SPLIT sweep (k_e_sweep) whose CTAs take (system,
+// i-block) work items of the unfinished systems from an atomic queue,
+// largest systems first.  The CTA that computed an i-block's forces runs
+// the step's next per-particle stage on that block (state copy, predictor,
+// corrector) and packs the FP32 records the next sweep reads; only the
+// step size, a minimum over the whole system, waits for the system's last
+// item.  A step is a fixed sequence of five launches and `batch` steps are
+// captured in a CUDA graph and replayed.  A
+// run is usually dominated by a few systems with hard binaries that need
 // thousands of tiny shared steps, so the step latency with few active
-// systems is what these fusions shorten.
+// systems is what the fused stages shorten.
 // Energies are fp64: an in-order fp64 Phi per system (same arithmetic and j
 // order as phi_kernel.c) and fp64 sums in fixed order.
 
@@ -25,22 +24,16 @@
 #include <string.h>
 
 #include <algorithm>
+#include <type_traits>
 #include <numeric>
 #include <vector>
 
 #include "tg_common.cuh"
 #include "tg_split_ops.cuh"
+#include "tg_tma.cuh"
 
 #define TG_EXPORT extern "C" __attribute__((visibility("default")))
 
-namespace tg {
-cudaError_t launch_split_batched(int kernel, const float4 *rec,
-                                 const uint64_t *off, const unsigned *order,
-                                 const int *active, unsigned n_sys,
-                                 unsigned *queue, void *const *out, double eta,
-                                 unsigned *err, int sms, cudaStream_t st,
-                                 const unsigned *n_dev, const uint2 *items);
-}  // namespace tg
 
 using namespace tg;
 
@@ -114,8 +107,12 @@ __device__ unsigned block_exclusive_scan(unsigned v, unsigned *wsum,
 __global__ void __launch_bounds__(COMPACT_NT)
 k_e_begin(SysCtl *c, int *active, const unsigned *order, const uint64_t *off,
           unsigned ns, const double *t_end_p, double eta, unsigned ctas,
-          unsigned *alist, unsigned *acount, uint2 *items, unsigned *icount)
+          unsigned *alist, unsigned *acount, uint2 *items, unsigned *icount,
+          unsigned *sys_items, unsigned *queues)
 {
+    // the work counters of the step's four sweeps (a kernel write instead
+    // of memset nodes in the step graph)
+    if (threadIdx.x < 4) queues[threadIdx.x] = 0;
     __shared__ unsigned wsum[COMPACT_NT / 32];
     __shared__ unsigned n_active;
     const int t = threadIdx.x;
@@ -146,6 +143,7 @@ k_e_begin(SysCtl *c, int *active, const unsigned *order, const uint64_t *off,
         const unsigned ipos = block_exclusive_scan(nb, wsum, &itot);
         if (on) {
             alist[sbase + spos] = s;
+            sys_items[s] = nb;
             for (unsigned q = 0; q < nb; ++q) {
                 const unsigned ib = q * IB, ie = ib + IB < n ? ib + IB : n;
                 items[ibase + ipos + q] = make_uint2(s, ib | (ie << 16));
@@ -184,86 +182,268 @@ __global__ void k_e_pack_all(EArrays A, uint64_t n, float4 *out)
         e_pack_one(A, out, i);
 }
 
-// One CTA per active system (strided over the list).
-#define FOR_ACTIVE_SYSTEM(s, b, e, alist, acount, off)                        \
-    for (unsigned a_ = blockIdx.x; a_ < *(acount); a_ += gridDim.x)          \
-        for (uint64_t s = (alist)[a_], b = (off)[s], e = (off)[s + 1]; s != ~0ull; \
-             s = ~0ull)
+// ---------------------------------------------------------------------------
+// Per-system epilogues, run by the CTA that completes a system's last work
+// item of a sweep (the other items' outputs are read through L2).
+// ---------------------------------------------------------------------------
+enum Epilogue { EPI_NONE = 0, EPI_STEP_SIZE, EPI_PREDICT, EPI_CORRECT,
+                EPI_CORRECT_END };
 
-// min |dt_a| of the system -> power-of-two step (integrator/__init__.py:
-// 59-78), and the copy of the state at the start of the step.
-__global__ void k_e_step_size(EArrays A, const uint64_t *off, SysCtl *c,
-                              const unsigned *alist, const unsigned *acount)
+// The step's per-particle stages on one i-block [b, e) of a system, run by
+// the CTA that computed the block's forces right after it (a particle's
+// update needs only its own forces).  Records go to a buffer the running
+// sweep does not read, so items of the same system still loading theirs
+// see the old state.
+
+// the copy of the state at the start of the step
+__device__ void epi_copy(const EArrays &A, uint64_t b, uint64_t e)
 {
-    __shared__ double red[8];
+    for (uint64_t i = b + threadIdx.x; i < e; i += blockDim.x)
+        for (int d = 0; d < 3; ++d) {
+            A.r0[d][i] = A.r[d][i];
+            A.v0[d][i] = A.v[d][i];
+        }
+}
+
+// min |dt_a| over the whole system -> power-of-two step (integrator/
+// __init__.py:59-78): run by the CTA that completes the system's last item
+// (the other items' outputs are read through L2).
+__device__ void epi_step_size(const EArrays &A, SysCtl *c, uint64_t s,
+                              uint64_t b, uint64_t e)
+{
+    __shared__ double red[32];
     const int t = threadIdx.x;
-    FOR_ACTIVE_SYSTEM(s, b, e, alist, acount, off)
-    {
-        double m = INFINITY;
-        for (uint64_t i = b + t; i < e; i += blockDim.x) {
-            m = fmin(m, fabs(A.dt[0][i]));
-            for (int d = 0; d < 3; ++d) {
-                A.r0[d][i] = A.r[d][i];
-                A.v0[d][i] = A.v[d][i];
-            }
-        }
-        for (int o = 16; o > 0; o >>= 1)
-            m = fmin(m, __shfl_xor_sync(0xffffffffu, m, o));
-        if ((t & 31) == 0) red[t >> 5] = m;
-        __syncthreads();
-        if (t == 0) {
-            for (int q = 1; q < (int)(blockDim.x >> 5); ++q) m = fmin(m, red[q]);
-            m = fmin(m, red[0]);
-            c[s].tau = e_block_tstep(m, c[s].t, c[s].tau);
-        }
-        __syncthreads();
+    double m = INFINITY;
+    for (uint64_t i = b + t; i < e; i += blockDim.x)
+        m = fmin(m, fabs(__ldcg(&A.dt[0][i])));
+    for (int o = 16; o > 0; o >>= 1)
+        m = fmin(m, __shfl_xor_sync(0xffffffffu, m, o));
+    if ((t & 31) == 0) red[t >> 5] = m;
+    __syncthreads();
+    if (t == 0) {
+        for (int q = 1; q < (int)(blockDim.x >> 5); ++q) m = fmin(m, red[q]);
+        c[s].tau = e_block_tstep(m, c[s].t, c[s].tau);
     }
+    __syncthreads();
 }
 
 // H4.epredict (hermite.py:83-88), then the records of the predicted state.
-__global__ void k_e_predict(EArrays A, const uint64_t *off, const SysCtl *c,
-                            float4 *rec, const unsigned *alist,
-                            const unsigned *acount)
+__device__ void epi_predict(const EArrays &A, const SysCtl *c, float4 *rec,
+                            uint64_t s, uint64_t b, uint64_t e)
 {
-    FOR_ACTIVE_SYSTEM(s, b, e, alist, acount, off)
-    {
-        const double tau = c[s].tau;
-        for (uint64_t i = b + threadIdx.x; i < e; i += blockDim.x) {
-            for (int d = 0; d < 3; ++d) {
-                const double a = A.f0[d][i], j = A.f0[3 + d][i], v = A.v[d][i];
-                A.r[d][i] = A.r[d][i] + ((j * tau / 3 + a) * tau / 2 + v) * tau;
-                A.v[d][i] = v + (j * tau / 2 + a) * tau;
+    const double tau = c[s].tau;
+    for (uint64_t i = b + threadIdx.x; i < e; i += blockDim.x) {
+        for (int d = 0; d < 3; ++d) {
+            const double a = A.f0[d][i], j = A.f0[3 + d][i], v = A.v[d][i];
+            A.r[d][i] = A.r[d][i] + ((j * tau / 3 + a) * tau / 2 + v) * tau;
+            A.v[d][i] = v + (j * tau / 2 + a) * tau;
+        }
+        e_pack_one(A, rec, i);
+    }
+}
+
+// H4.ecorrect (hermite.py:96-119), then the records of the corrected state.
+__device__ void epi_correct(const EArrays &A, const SysCtl *c, float4 *rec,
+                            uint64_t s, uint64_t b, uint64_t e)
+{
+    const double tau = c[s].tau;
+    for (uint64_t i = b + threadIdx.x; i < e; i += blockDim.x) {
+        for (int d = 0; d < 3; ++d) {
+            const double a0 = A.f0[d][i], a1 = A.f1[d][i];
+            const double j0 = A.f0[3 + d][i], j1 = A.f1[3 + d][i];
+            const double v0 = A.v0[d][i], r0 = A.r0[d][i];
+            const double v1 = (((j0 - j1) * tau / 6 + (a0 + a1)) * tau / 2 + v0);
+            A.v[d][i] = v1;
+            A.r[d][i] = (((a0 - a1) * tau / 6 + (v0 + v1)) * tau / 2 + r0);
+        }
+        e_pack_one(A, rec, i);
+    }
+}
+
+// ---------------------------------------------------------------------------
+// Batched SPLIT sweep over the (system, i-block) work items of the active
+// systems, one persistent launch per force evaluation.  CTAs take items
+// from an atomic queue (largest systems first), stage the system's packed
+// records in shared memory with one bulk copy, and give each i (or packed i
+// pair) `lanes` threads that split the j loop and combine through shuffles.
+// The CTA that completes the last item of a system runs the step's next
+// per-system stage (the epilogue), so a Hermite step is five launches.
+// ---------------------------------------------------------------------------
+constexpr int BATCH_NT = 256;
+constexpr int BATCH_MAXN = 512;           // largest system held in smem
+
+struct BatchLaunch {
+    const float4 *rec;        // packed records of all systems
+    const uint64_t *off;      // n_sys + 1 offsets
+    const uint2 *items;       // (system, ib | ie << 16) per item
+    const unsigned *n_items;  // item count (device)
+    unsigned *queue;          // work counter (zeroed before the launch)
+    unsigned *sys_done;       // items finished per system (self-resetting)
+    const unsigned *sys_items;// items per system this step
+    double *out[MAX_OUT];
+    float eta;
+    double eta_d;
+    unsigned *err;
+    int epi;
+    EArrays A;
+    SysCtl *ctl;
+    float4 *rec_out;          // records written by the epilogues
+};
+
+// One system's i-range [ib, ib + ni) against all of its j.
+template <class Op, bool X2>
+__device__ __forceinline__ void batched_block(const BatchLaunch &L,
+                                              const float4 *rec, uint64_t b,
+                                              int n, int ib, int ni)
+{
+    constexpr int NF = Op::NF, NO = Op::NO, MAXC = Op::MAXC;
+    constexpr int NI = X2 ? 2 : 1;               // i per thread
+    const int tid = threadIdx.x;
+    const int units = (ni + NI - 1) / NI;        // i (pairs) of the block
+    int lanes = 1;
+    while (lanes < 32 && lanes * 2 * units <= BATCH_NT) lanes *= 2;
+    const int groups = BATCH_NT / lanes;
+    const int lane = tid % lanes;
+    for (int u0 = tid / lanes; u0 - tid / lanes < units; u0 += groups) {
+        const int u = u0 < units ? u0 : units - 1;
+        int iv[NI];
+#pragma unroll
+        for (int k = 0; k < NI; ++k) {
+            const int q = u * NI + k;
+            iv[k] = ib + (q < ni ? q : ni - 1);
+        }
+        float sum[NI][NO], corr[NI][NO], part[NI][NO];
+#pragma unroll
+        for (int k = 0; k < NI; ++k)
+#pragma unroll
+            for (int c = 0; c < NO; ++c) sum[k][c] = corr[k][c] = part[k][c] = 0.f;
+        auto fold = [&]() {
+#pragma unroll
+            for (int k = 0; k < NI; ++k)
+#pragma unroll
+                for (int c = 0; c < NO; ++c) {
+                    if (c == MAXC) sum[k][c] = fmaxf(sum[k][c], part[k][c]);
+                    else kahan_add(sum[k][c], corr[k][c], part[k][c]);
+                    part[k][c] = 0.f;
+                }
+        };
+        if constexpr (X2) {
+            using OpX2 = typename X2Of<Op>::type;
+            const typename OpX2::I ip2 = OpX2::pack(
+                Op::load(rec + iv[0] * NF), Op::load(rec + iv[1] * NF));
+            for (int j0 = lane; j0 < n; j0 += 16 * lanes) {
+                float2 p2[NO];
+#pragma unroll
+                for (int c = 0; c < NO; ++c) p2[c] = make_float2(0.f, 0.f);
+                const int je = j0 + 16 * lanes < n ? j0 + 16 * lanes : n;
+                for (int j = j0; j < je; j += lanes)
+                    OpX2::pair(ip2, Op::load(rec + j * NF), p2, L.eta);
+#pragma unroll
+                for (int c = 0; c < NO; ++c) {
+                    part[0][c] = p2[c].x;
+                    part[NI - 1][c] = p2[c].y;
+                }
+                fold();
             }
-            e_pack_one(A, rec, i);
+        } else {
+            const typename Op::P ip = Op::load(rec + iv[0] * NF);
+            for (int j0 = lane; j0 < n; j0 += 16 * lanes) {
+                const int je = j0 + 16 * lanes < n ? j0 + 16 * lanes : n;
+                for (int j = j0; j < je; j += lanes)
+                    Op::pair(ip, Op::load(rec + j * NF), part[0], L.eta);
+                fold();
+            }
+        }
+#pragma unroll
+        for (int k = 0; k < NI; ++k) {
+            double v[NO];
+#pragma unroll
+            for (int c = 0; c < NO; ++c) {
+                v[c] = (c == MAXC) ? (double)sum[k][c]
+                                   : (double)sum[k][c] - (double)corr[k][c];
+                for (int o = lanes / 2; o > 0; o >>= 1) {
+                    double w = __shfl_xor_sync(0xffffffffu, v[c], o, lanes);
+                    v[c] = (c == MAXC) ? fmax(v[c], w) : v[c] + w;
+                }
+            }
+            const int q = u0 * NI + k;
+            if (lane == 0 && u0 < units && q < ni) {
+                Op::finish(v, L.eta_d);
+#pragma unroll
+                for (int c = 0; c < NO; ++c) L.out[c][b + iv[k]] = v[c];
+            }
         }
     }
 }
 
-// H4.ecorrect (hermite.py:96-119), the records of the corrected state and,
-// after the last pass, the end of the system's step (t += tau).
-__global__ void k_e_correct(EArrays A, const uint64_t *off, SysCtl *c,
-                            float4 *rec, const unsigned *alist,
-                            const unsigned *acount, int last)
+template <class Op>
+__global__ void __launch_bounds__(BATCH_NT, 2)
+k_e_sweep(const BatchLaunch L)
 {
-    FOR_ACTIVE_SYSTEM(s, b, e, alist, acount, off)
-    {
-        const double tau = c[s].tau;
-        for (uint64_t i = b + threadIdx.x; i < e; i += blockDim.x) {
-            for (int d = 0; d < 3; ++d) {
-                const double a0 = A.f0[d][i], a1 = A.f1[d][i];
-                const double j0 = A.f0[3 + d][i], j1 = A.f1[3 + d][i];
-                const double v0 = A.v0[d][i], r0 = A.r0[d][i];
-                const double v1 =
-                    (((j0 - j1) * tau / 6 + (a0 + a1)) * tau / 2 + v0);
-                A.v[d][i] = v1;
-                A.r[d][i] = (((a0 - a1) * tau / 6 + (v0 + v1)) * tau / 2 + r0);
+    constexpr int NF = Op::NF;
+    constexpr bool X2 = !std::is_void<typename X2Of<Op>::type>::value;
+    __shared__ __align__(128) float4 rec[BATCH_MAXN * NF];
+    __shared__ __align__(8) uint64_t bar;
+    __shared__ unsigned item;
+    __shared__ int last;
+    const int tid = threadIdx.x;
+    if (tid == 0) {
+        mbar_init(&bar, 1);
+        mbar_init_fence();
+    }
+    __syncthreads();
+    const unsigned n_items = *L.n_items;
+    uint32_t phase = 0;
+    for (;;) {
+        if (tid == 0) item = atomicAdd(L.queue, 1u);
+        __syncthreads();
+        const unsigned w = item;
+        if (w >= n_items) break;
+        const unsigned sys = L.items[w].x;
+        const uint64_t b = L.off[sys];
+        const int n = (int)(L.off[sys + 1] - b);
+        const int ib = (int)(L.items[w].y & 0xffffu);
+        const int ie = (int)(L.items[w].y >> 16);
+        if (n > BATCH_MAXN || ie > n || ib >= ie) {
+            if (tid == 0) atomicOr(L.err, (unsigned)DERR_BAD_LAUNCH);
+            break;
+        }
+        if (tid == 0) {
+            const uint32_t bytes = (uint32_t)(n * NF * sizeof(float4));
+            mbar_arrive_expect_tx(&bar, bytes);
+            bulk_g2s(rec, L.rec + b * NF, bytes, &bar);
+        }
+        bool got = mbar_wait_bounded(&bar, phase, L.err);
+        phase ^= 1u;
+        if (!__syncthreads_and(got)) break;
+        batched_block<Op, X2>(L, rec, b, n, ib, ie - ib);
+        __syncthreads();   // this block's forces are written (CTA scope)
+        const uint64_t bi = b + ib, ei = b + ie;
+        if (L.epi == EPI_STEP_SIZE) {
+            epi_copy(L.A, bi, ei);
+            // publish this item's Tstep outputs, then count it; the CTA
+            // that completes the system takes the system's minimum
+            __threadfence();
+            __syncthreads();
+            if (tid == 0)
+                last = atomicAdd(&L.sys_done[sys], 1u) + 1u == L.sys_items[sys];
+            __syncthreads();
+            if (last) {
+                __threadfence();
+                epi_step_size(L.A, L.ctl, sys, b, b + n);
+                if (tid == 0) L.sys_done[sys] = 0;
             }
-            e_pack_one(A, rec, i);
+        } else if (L.epi == EPI_PREDICT) {
+            epi_predict(L.A, L.ctl, L.rec_out, sys, bi, ei);
+        } else if (L.epi == EPI_CORRECT || L.epi == EPI_CORRECT_END) {
+            epi_correct(L.A, L.ctl, L.rec_out, sys, bi, ei);
+            // the system's time moves once, by its first item
+            if (L.epi == EPI_CORRECT_END && ib == 0 && tid == 0) {
+                L.ctl[sys].t += L.ctl[sys].tau;
+                L.ctl[sys].nsteps += 1;
+            }
         }
-        if (last && threadIdx.x == 0) {
-            c[s].t += tau;
-            c[s].nsteps += 1;
-        }
+        __syncthreads();   // the records of this system are no longer read
     }
 }
 
@@ -323,10 +503,12 @@ struct Ensemble {
     unsigned *acount = nullptr;
     uint2 *items = nullptr;         // their i-blocks, same order
     unsigned *icount = nullptr;
+    unsigned *sys_items = nullptr;  // items per system this step
+    unsigned *sys_done = nullptr;   // items finished per system
     SysCtl *ctl = nullptr;
-    unsigned *queue = nullptr;
+    unsigned *queue = nullptr;      // work counters of the four sweeps
     unsigned *err = nullptr;
-    float4 *pack = nullptr;
+    float4 *pack = nullptr;         // three record buffers of n x 3 float4
     double *ke = nullptr, *pe = nullptr;
     double t_end = 0.0;
     double *d_tend = nullptr;       // t_end of the current evolve call
@@ -342,44 +524,63 @@ unsigned grid_for(uint64_t n, int sms)
     return (unsigned)(b < 1 ? 1 : (b > cap ? cap : b));
 }
 
-// One force evaluation of every active system from the current records:
-// one persistent batched sweep over the (system, i-block) items.
-cudaError_t e_forces(Ensemble *E, double *const *out, int kernel, double eta)
+// One force evaluation of every active system from the current records,
+// followed per system by the epilogue `epi`.
+cudaError_t e_sweep(Ensemble *E, int kernel, double *const *out, double eta,
+                    int epi, int read_buf, int write_buf, int queue)
 {
-    return launch_split_batched(kernel, E->pack, E->off, E->alist, E->active,
-                                E->ns, E->queue, (void *const *)out, eta,
-                                E->err, E->sms, E->stream, E->icount,
-                                E->items);
+    BatchLaunch L;
+    memset(&L, 0, sizeof(L));
+    L.rec = E->pack + (size_t)read_buf * E->n * 3;
+    L.off = E->off;
+    L.items = E->items;
+    L.n_items = E->icount;
+    L.queue = E->queue + queue;
+    L.sys_done = E->sys_done;
+    L.sys_items = E->sys_items;
+    for (int c = 0; c < n_out(kernel); ++c) L.out[c] = out[c];
+    L.eta = (float)eta;
+    L.eta_d = eta;
+    L.err = E->err;
+    L.epi = epi;
+    L.A = E->A;
+    L.ctl = E->ctl;
+    L.rec_out = E->pack + (size_t)write_buf * E->n * 3;
+    // persistent CTAs; a system of up to 512 particles is at most 16 items
+    const uint64_t max_items = (uint64_t)E->ns * 16;
+    const unsigned grid = (unsigned)((uint64_t)E->sms * 2 < max_items
+                                         ? (uint64_t)E->sms * 2 : max_items);
+    if (kernel == K_TSTEP)
+        k_e_sweep<TstepS><<<grid, BATCH_NT, 0, E->stream>>>(L);
+    else
+        k_e_sweep<AccJerkS><<<grid, BATCH_NT, 0, E->stream>>>(L);
+    g_launch_count += 1;
+    return cudaGetLastError();
 }
 
 // One Hermite-4 step of every unfinished system (hermite.py:390-410 with
-// epec(2)): nine launches.  The records packed by the kernel that produced
-// the state feed the next sweep, so the step's first two sweeps (Tstep and
-// the forces at the start) share the records left by the previous step.
+// epec(2)): the step start and compaction, then four sweeps whose
+// epilogues set the step size, predict, and correct twice.  Records rotate
+// through three buffers (state A -> predicted B -> corrected C -> final A)
+// so that no sweep writes the buffer it reads, and every step starts from
+// buffer 0.
 cudaError_t e_step(Ensemble *E)
 {
     cudaStream_t st = E->stream;
-    const unsigned ga = (unsigned)E->sms * 4;   // CTAs over active systems
     k_e_begin<<<1, COMPACT_NT, 0, st>>>(E->ctl, E->active, E->order, E->off,
                                         E->ns, E->d_tend, E->eta,
                                         (unsigned)E->sms * 2, E->alist,
-                                        E->acount, E->items, E->icount);
-    cudaError_t e = e_forces(E, E->A.dt, K_TSTEP, E->eta);
-    if (e != cudaSuccess) return e;
-    k_e_step_size<<<ga, 256, 0, st>>>(E->A, E->off, E->ctl, E->alist,
-                                      E->acount);
-    e = e_forces(E, E->A.f0, K_ACC_JERK, 0.0);
-    if (e != cudaSuccess) return e;
-    k_e_predict<<<ga, 256, 0, st>>>(E->A, E->off, E->ctl, E->pack, E->alist,
-                                    E->acount);
-    for (int pass = 0; pass < 2; ++pass) {
-        e = e_forces(E, E->A.f1, K_ACC_JERK, 0.0);
-        if (e != cudaSuccess) return e;
-        k_e_correct<<<ga, 256, 0, st>>>(E->A, E->off, E->ctl, E->pack,
-                                        E->alist, E->acount, pass == 1);
-    }
-    g_launch_count += 5;
-    return cudaGetLastError();
+                                        E->acount, E->items, E->icount,
+                                        E->sys_items, E->queue);
+    g_launch_count += 1;
+    cudaError_t e = e_sweep(E, K_TSTEP, E->A.dt, E->eta, EPI_STEP_SIZE, 0, 0, 0);
+    if (e == cudaSuccess)
+        e = e_sweep(E, K_ACC_JERK, E->A.f0, 0.0, EPI_PREDICT, 0, 1, 1);
+    if (e == cudaSuccess)
+        e = e_sweep(E, K_ACC_JERK, E->A.f1, 0.0, EPI_CORRECT, 1, 2, 2);
+    if (e == cudaSuccess)
+        e = e_sweep(E, K_ACC_JERK, E->A.f1, 0.0, EPI_CORRECT_END, 2, 0, 3);
+    return e;
 }
 
 }  // namespace
@@ -448,9 +649,9 @@ TG_EXPORT int tupan_gb300_ensemble_create(unsigned n_sys,
         cudaMalloc((void **)&E->order, n_sys * sizeof(unsigned)) != cudaSuccess ||
         cudaMalloc((void **)&E->active, n_sys * sizeof(int)) != cudaSuccess ||
         cudaMalloc((void **)&E->ctl, n_sys * sizeof(SysCtl)) != cudaSuccess ||
-        cudaMalloc((void **)&E->queue, sizeof(unsigned)) != cudaSuccess ||
+        cudaMalloc((void **)&E->queue, 4 * sizeof(unsigned)) != cudaSuccess ||
         cudaMalloc((void **)&E->err, sizeof(unsigned)) != cudaSuccess ||
-        cudaMalloc((void **)&E->pack, n * 3 * sizeof(float4)) != cudaSuccess ||
+        cudaMalloc((void **)&E->pack, 3 * n * 3 * sizeof(float4)) != cudaSuccess ||
         cudaMalloc((void **)&E->ke, n_sys * sizeof(double)) != cudaSuccess ||
         cudaMalloc((void **)&E->pe, n_sys * sizeof(double)) != cudaSuccess ||
         cudaMalloc((void **)&E->alist, n_sys * sizeof(unsigned)) != cudaSuccess ||
@@ -458,10 +659,14 @@ TG_EXPORT int tupan_gb300_ensemble_create(unsigned n_sys,
         cudaMalloc((void **)&E->items, (size_t)n_sys * 16 * sizeof(uint2)) !=
             cudaSuccess ||
         cudaMalloc((void **)&E->icount, sizeof(unsigned)) != cudaSuccess ||
+        cudaMalloc((void **)&E->sys_items, n_sys * sizeof(unsigned)) != cudaSuccess ||
+        cudaMalloc((void **)&E->sys_done, n_sys * sizeof(unsigned)) != cudaSuccess ||
         cudaMalloc((void **)&E->d_tend, sizeof(double)) != cudaSuccess)
         return ST_CUDA;
     cudaMemset(E->acount, 0, sizeof(unsigned));
     cudaMemset(E->icount, 0, sizeof(unsigned));
+    cudaMemset(E->sys_items, 0, n_sys * sizeof(unsigned));
+    cudaMemset(E->sys_done, 0, n_sys * sizeof(unsigned));
     cudaMemcpy(A.sys, sys.data(), n * sizeof(unsigned), cudaMemcpyHostToDevice);
     cudaMemcpy(E->off, sys_off, (n_sys + 1) * sizeof(uint64_t),
                cudaMemcpyHostToDevice);
@@ -603,6 +808,8 @@ TG_EXPORT int tupan_gb300_ensemble_destroy(void *handle)
     cudaFree(E->acount);
     cudaFree(E->items);
     cudaFree(E->icount);
+    cudaFree(E->sys_items);
+    cudaFree(E->sys_done);
     cudaFree(E->d_tend);
     cudaFree(E->active);
     cudaFree(E->ctl);

@@ -202,4 +202,254 @@ struct SnapS {
     __device__ static void finish(double *, double) {}
 };
 
+// Kahan-compensated FP32 accumulation of one run of pair terms.
+__device__ __forceinline__ void kahan_add(float &sum, float &corr, float x)
+{
+    float y = x - corr;
+    float t = sum + y;
+    corr = (t - sum) - y;
+    sum = t;
+}
+
+// ---------------------------------------------------------------------------
+// Two i-particles per thread in packed FP32 (f32x2: .x first i, .y second).
+// One FFMA2/FADD2/FMUL2 does the same operation for both i against the same
+// j, halving the instructions issued per interaction so that the FMA pipe,
+// not instruction issue, bounds the sweep.  i-side positions and velocities
+// are kept negated so that every difference is an addition.
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ float2 dup(float a) { return make_float2(a, a); }
+__device__ __forceinline__ float2 add2(float2 a, float2 b) { return __fadd2_rn(a, b); }
+__device__ __forceinline__ float2 mul2(float2 a, float2 b) { return __fmul2_rn(a, b); }
+__device__ __forceinline__ float2 fma2(float2 a, float2 b, float2 c) { return __ffma2_rn(a, b, c); }
+
+struct PosI2 { float2 nxh, nyh, nzh, nxl, nyl, nzl, e2; };
+struct PosVelI2 { float2 nxh, nyh, nzh, nxl, nyl, nzl, e2, nvx, nvy, nvz; };
+
+// rsqrt with one Newton step on both lanes: y (3/2 - s y^2 / 2), masked to 0
+// where s == h2 (r2 == 0: self pairs and coincident particles).
+__device__ __forceinline__ float2 rsqrt_nr2(float2 s, float2 h2)
+{
+    float2 y = make_float2(rsqrtf(s.x), rsqrtf(s.y));
+    float2 u = mul2(mul2(s, y), y);
+    y = mul2(y, fma2(u, dup(-0.5f), dup(1.5f)));
+    y.x = (s.x > h2.x) ? y.x : 0.0f;
+    y.y = (s.y > h2.y) ? y.y : 0.0f;
+    return y;
+}
+
+struct PhiS2 {
+    using P = PhiS::P;
+    using I = PosI2;
+    __device__ static I pack(const P &a, const P &b)
+    {
+        return {make_float2(-a.xh, -b.xh), make_float2(-a.yh, -b.yh),
+                make_float2(-a.zh, -b.zh), make_float2(-a.xl, -b.xl),
+                make_float2(-a.yl, -b.yl), make_float2(-a.zl, -b.zl),
+                make_float2(a.e2, b.e2)};
+    }
+    __device__ static void pair(const I &i, const P &j, float2 *acc, float)
+    {
+        float2 dx = add2(add2(dup(j.xh), i.nxh), add2(dup(j.xl), i.nxl));
+        float2 dy = add2(add2(dup(j.yh), i.nyh), add2(dup(j.yl), i.nyl));
+        float2 dz = add2(add2(dup(j.zh), i.nzh), add2(dup(j.zl), i.nzl));
+        float2 h2 = add2(i.e2, dup(j.e2));
+        float2 s = fma2(dz, dz, fma2(dy, dy, fma2(dx, dx, h2)));
+        float2 y = rsqrt_nr2(s, h2);
+        acc[0] = fma2(dup(-j.m), y, acc[0]);
+    }
+};
+
+struct AccS2 {
+    using P = PhiS::P;
+    using I = PosI2;
+    __device__ static I pack(const P &a, const P &b) { return PhiS2::pack(a, b); }
+    __device__ static void pair(const I &i, const P &j, float2 *acc, float)
+    {
+        float2 dx = add2(add2(dup(j.xh), i.nxh), add2(dup(j.xl), i.nxl));
+        float2 dy = add2(add2(dup(j.yh), i.nyh), add2(dup(j.yl), i.nyl));
+        float2 dz = add2(add2(dup(j.zh), i.nzh), add2(dup(j.zl), i.nzl));
+        float2 h2 = add2(i.e2, dup(j.e2));
+        float2 s = fma2(dz, dz, fma2(dy, dy, fma2(dx, dx, h2)));
+        float2 y = rsqrt_nr2(s, h2);
+        float2 mk = mul2(mul2(dup(j.m), y), mul2(y, y));
+        acc[0] = fma2(mk, dx, acc[0]);
+        acc[1] = fma2(mk, dy, acc[1]);
+        acc[2] = fma2(mk, dz, acc[2]);
+    }
+};
+
+struct AccJerkS2 {
+    using P = AccJerkS::P;
+    using I = PosVelI2;
+    __device__ static I pack(const P &a, const P &b)
+    {
+        return {make_float2(-a.xh, -b.xh), make_float2(-a.yh, -b.yh),
+                make_float2(-a.zh, -b.zh), make_float2(-a.xl, -b.xl),
+                make_float2(-a.yl, -b.yl), make_float2(-a.zl, -b.zl),
+                make_float2(a.e2, b.e2),   make_float2(-a.vx, -b.vx),
+                make_float2(-a.vy, -b.vy), make_float2(-a.vz, -b.vz)};
+    }
+    __device__ static void pair(const I &i, const P &j, float2 *acc, float)
+    {
+        float2 dx = add2(add2(dup(j.xh), i.nxh), add2(dup(j.xl), i.nxl));
+        float2 dy = add2(add2(dup(j.yh), i.nyh), add2(dup(j.yl), i.nyl));
+        float2 dz = add2(add2(dup(j.zh), i.nzh), add2(dup(j.zl), i.nzl));
+        float2 ux = add2(dup(j.vx), i.nvx);
+        float2 uy = add2(dup(j.vy), i.nvy);
+        float2 uz = add2(dup(j.vz), i.nvz);
+        float2 h2 = add2(i.e2, dup(j.e2));
+        float2 s = fma2(dz, dz, fma2(dy, dy, fma2(dx, dx, h2)));
+        float2 rv = fma2(dz, uz, fma2(dy, uy, mul2(dx, ux)));
+        float2 y = rsqrt_nr2(s, h2);
+        float2 y2 = mul2(y, y);
+        float2 mk = mul2(mul2(dup(j.m), y), y2);
+        float2 nal = mul2(mul2(rv, dup(-3.0f)), y2);
+        acc[0] = fma2(mk, dx, acc[0]);
+        acc[1] = fma2(mk, dy, acc[1]);
+        acc[2] = fma2(mk, dz, acc[2]);
+        acc[3] = fma2(mk, fma2(nal, dx, ux), acc[3]);
+        acc[4] = fma2(mk, fma2(nal, dy, uy), acc[4]);
+        acc[5] = fma2(mk, fma2(nal, dz, uz), acc[5]);
+    }
+};
+
+// Tstep on both lanes (TstepS's arithmetic); the i image also carries m.
+struct PosVelMI2 {
+    float2 nxh, nyh, nzh, nxl, nyl, nzl, e2, nvx, nvy, nvz, m;
+};
+
+__device__ __forceinline__ float2 rsqrt_nr2_raw(float2 s)
+{
+    float2 y = make_float2(rsqrtf(s.x), rsqrtf(s.y));
+    float2 u = mul2(mul2(s, y), y);
+    return mul2(y, fma2(u, dup(-0.5f), dup(1.5f)));
+}
+
+struct TstepS2 {
+    using P = AccJerkS::P;
+    using I = PosVelMI2;
+    __device__ static I pack(const P &a, const P &b)
+    {
+        return {make_float2(-a.xh, -b.xh), make_float2(-a.yh, -b.yh),
+                make_float2(-a.zh, -b.zh), make_float2(-a.xl, -b.xl),
+                make_float2(-a.yl, -b.yl), make_float2(-a.zl, -b.zl),
+                make_float2(a.e2, b.e2),   make_float2(-a.vx, -b.vx),
+                make_float2(-a.vy, -b.vy), make_float2(-a.vz, -b.vz),
+                make_float2(a.m, b.m)};
+    }
+    __device__ static void pair(const I &i, const P &j, float2 *acc, float eta)
+    {
+        float2 dx = add2(add2(dup(j.xh), i.nxh), add2(dup(j.xl), i.nxl));
+        float2 dy = add2(add2(dup(j.yh), i.nyh), add2(dup(j.yl), i.nyl));
+        float2 dz = add2(add2(dup(j.zh), i.nzh), add2(dup(j.zl), i.nzl));
+        float2 ux = add2(dup(j.vx), i.nvx);
+        float2 uy = add2(dup(j.vy), i.nvy);
+        float2 uz = add2(dup(j.vz), i.nvz);
+        float2 h2 = add2(i.e2, dup(j.e2));
+        float2 msum = add2(i.m, dup(j.m));
+        float2 s = fma2(dz, dz, fma2(dy, dy, fma2(dx, dx, h2)));
+        float2 rv = fma2(dz, uz, fma2(dy, uy, mul2(dx, ux)));
+        float2 v2 = fma2(uz, uz, fma2(uy, uy, mul2(ux, ux)));
+        float2 y = rsqrt_nr2_raw(s);
+        float2 q = mul2(y, y);
+        float2 phi = mul2(msum, y);
+        float2 w2 = mul2(q, fma2(dup(2.0f), phi, v2));
+        float2 g = mul2(q, fma2(mul2(dup(2.0f), q), phi, w2));
+        g = mul2(g, mul2(dup(eta), rsqrt_nr2_raw(w2)));
+        w2 = fma2(make_float2(-g.x, -g.y), rv, w2);
+        w2.x = (s.x > h2.x) ? w2.x : 0.0f;
+        w2.y = (s.y > h2.y) ? w2.y : 0.0f;
+        acc[0] = add2(acc[0], w2);
+        acc[1] = make_float2(fmaxf(w2.x, acc[1].x), fmaxf(w2.y, acc[1].y));
+    }
+};
+
+// Snap and crackle on both lanes (SnapS's arithmetic).
+struct SnapI2 {
+    float2 nxh, nyh, nzh, nxl, nyl, nzl, e2, nvx, nvy, nvz, nax, nay, naz,
+        njx, njy, njz;
+};
+
+struct SnapS2 {
+    using P = SnapS::P;
+    using I = SnapI2;
+    __device__ static I pack(const P &a, const P &b)
+    {
+        return {make_float2(-a.xh, -b.xh), make_float2(-a.yh, -b.yh),
+                make_float2(-a.zh, -b.zh), make_float2(-a.xl, -b.xl),
+                make_float2(-a.yl, -b.yl), make_float2(-a.zl, -b.zl),
+                make_float2(a.e2, b.e2),   make_float2(-a.vx, -b.vx),
+                make_float2(-a.vy, -b.vy), make_float2(-a.vz, -b.vz),
+                make_float2(-a.ax, -b.ax), make_float2(-a.ay, -b.ay),
+                make_float2(-a.az, -b.az), make_float2(-a.jx, -b.jx),
+                make_float2(-a.jy, -b.jy), make_float2(-a.jz, -b.jz)};
+    }
+    __device__ static void pair(const I &i, const P &j, float2 *acc, float)
+    {
+        float2 dx = add2(add2(dup(j.xh), i.nxh), add2(dup(j.xl), i.nxl));
+        float2 dy = add2(add2(dup(j.yh), i.nyh), add2(dup(j.yl), i.nyl));
+        float2 dz = add2(add2(dup(j.zh), i.nzh), add2(dup(j.zl), i.nzl));
+        float2 ux = add2(dup(j.vx), i.nvx);
+        float2 uy = add2(dup(j.vy), i.nvy);
+        float2 uz = add2(dup(j.vz), i.nvz);
+        float2 Ax = add2(dup(j.ax), i.nax);
+        float2 Ay = add2(dup(j.ay), i.nay);
+        float2 Az = add2(dup(j.az), i.naz);
+        float2 Jx = add2(dup(j.jx), i.njx);
+        float2 Jy = add2(dup(j.jy), i.njy);
+        float2 Jz = add2(dup(j.jz), i.njz);
+        float2 h2 = add2(i.e2, dup(j.e2));
+        float2 s = fma2(dz, dz, fma2(dy, dy, fma2(dx, dx, h2)));
+        float2 rv = fma2(dz, uz, fma2(dy, uy, mul2(dx, ux)));
+        float2 v2 = fma2(uz, uz, fma2(uy, uy, mul2(ux, ux)));
+        float2 rJ = fma2(dz, Jz, fma2(dy, Jy, mul2(dx, Jx)));
+        float2 rA = fma2(dz, Az, fma2(dy, Ay, mul2(dx, Ax)));
+        float2 vA = fma2(uz, Az, fma2(uy, Ay, mul2(ux, Ax)));
+        float2 y = rsqrt_nr2(s, h2);
+        float2 q = mul2(y, y);
+        float2 al = mul2(rv, q);
+        float2 al2 = mul2(al, al);
+        float2 be = mul2(dup(3.0f), fma2(add2(v2, rA), q, al2));
+        float2 ga = fma2(fma2(dup(3.0f), vA, rJ), q,
+                         mul2(al, fma2(dup(-4.0f), al2, be)));
+        al = mul2(al, dup(3.0f));
+        ga = mul2(ga, dup(3.0f));
+        const float2 nal = make_float2(-al.x, -al.y);
+        ux = fma2(nal, dx, ux);
+        uy = fma2(nal, dy, uy);
+        uz = fma2(nal, dz, uz);
+        float2 two_al = mul2(dup(2.0f), al);
+        float2 tx = fma2(two_al, ux, mul2(be, dx));
+        float2 ty = fma2(two_al, uy, mul2(be, dy));
+        float2 tz = fma2(two_al, uz, mul2(be, dz));
+        Ax = add2(Ax, make_float2(-tx.x, -tx.y));
+        Ay = add2(Ay, make_float2(-ty.x, -ty.y));
+        Az = add2(Az, make_float2(-tz.x, -tz.y));
+        al = mul2(al, dup(3.0f));
+        be = mul2(be, dup(3.0f));
+        float2 kx = fma2(al, Ax, fma2(be, ux, mul2(ga, dx)));
+        float2 ky = fma2(al, Ay, fma2(be, uy, mul2(ga, dy)));
+        float2 kz = fma2(al, Az, fma2(be, uz, mul2(ga, dz)));
+        Jx = add2(Jx, make_float2(-kx.x, -kx.y));
+        Jy = add2(Jy, make_float2(-ky.x, -ky.y));
+        Jz = add2(Jz, make_float2(-kz.x, -kz.y));
+        float2 mk = mul2(mul2(dup(j.m), y), q);
+        acc[0] = fma2(mk, Ax, acc[0]);
+        acc[1] = fma2(mk, Ay, acc[1]);
+        acc[2] = fma2(mk, Az, acc[2]);
+        acc[3] = fma2(mk, Jx, acc[3]);
+        acc[4] = fma2(mk, Jy, acc[4]);
+        acc[5] = fma2(mk, Jz, acc[5]);
+    }
+};
+
+// Packed-pair partner of each scalar operator (void: none).
+template <class Op> struct X2Of { using type = void; };
+template <> struct X2Of<PhiS> { using type = PhiS2; };
+template <> struct X2Of<AccS> { using type = AccS2; };
+template <> struct X2Of<AccJerkS> { using type = AccJerkS2; };
+template <> struct X2Of<TstepS> { using type = TstepS2; };
+template <> struct X2Of<SnapS> { using type = SnapS2; };
+
 }  // namespace tg
