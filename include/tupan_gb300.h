@@ -324,13 +324,14 @@ int tupan_gb300_kepler_pairs(uint64_t n, double dt, const double *m,
  * the kernel's order (m, rx, ry, rz, e2, vx, vy, vz), outs 6 (drx .. dvz);
  * flag -1 or +1.  *n_kepler (host) receives the number of queued pairs;
  * kepler_iters (host, 65 bins, may be NULL) accumulates their update
- * counts.  Synchronous. */
+ * counts.  mode 0 EXACT; 1 SPLIT: leapfrog-branch pairs in FP32 on
+ * double-single positions, the Kepler branch in fp64.  Synchronous. */
 int tupan_gb300_sakura_queue(uint64_t ni, const void *const *i_attrs,
                              uint64_t nj, const void *const *j_attrs,
                              double dt, int64_t flag, void *const *outs,
                              int use_mlp, long long budget, void *stream,
                              unsigned long long *n_kepler,
-                             long long *kepler_iters);
+                             long long *kepler_iters, int mode);
 /* Device-resident Sakura integrator (tupan/integrator/sakura.py:100-117,
  * fixed step): drift tau/2, two queued Sakura half-sweeps, drift tau/2. */
 int tupan_gb300_sakura_create(uint64_t n, const double *m, const double *e2,
@@ -342,6 +343,8 @@ int tupan_gb300_sakura_evolve(void *handle, double tau, double t_end,
                               int use_mlp, double *t_out,
                               long long *steps_out, long long *kepler_out,
                               long long *kepler_iters);
+/* The integrator's Sakura sweeps: mode 0 EXACT (default), 1 SPLIT. */
+int tupan_gb300_sakura_set_mode(void *handle, int mode);
 int tupan_gb300_sakura_get_state(void *handle, double *rx, double *ry,
                                  double *rz, double *vx, double *vy,
                                  double *vz);

@@ -82,3 +82,50 @@ def test_device_sakura_integrator_matches_oracle():
     for c in ("rx", "ry", "rz", "vx", "vy", "vz"):
         scale = np.abs(ref[c]).max()
         assert np.max(np.abs(got[c] - ref[c])) <= 1e-11 * scale, c
+
+
+@pytest.mark.parametrize("flag", [-1, 1])
+@pytest.mark.parametrize("eps", [0.0, 1e-3])
+def test_sakura_queue_split_close_to_oracle(flag, eps):
+    """SPLIT mode: the leapfrog-branch pairs in FP32 on double-single
+    positions (closed-form increments), the Kepler branch in fp64."""
+    torch = pytest.importorskip("torch")
+    n = 2048
+    ps = ics.plummer(n, eps=eps, seed=6, masses="salpeter")
+    d = _dev(ps, torch)
+    ptr = [d[k].data_ptr() for k in NAMES]
+    out = [torch.zeros(n, dtype=torch.float64, device="cuda")
+           for _ in range(6)]
+    dt = 1.0 / 512
+    nk_s, _ = kp.sakura_queue(n, ptr, n, ptr, [o.data_ptr() for o in out],
+                              dt, flag, mode="split")
+    nk_e, _ = kp.sakura_queue(n, ptr, n, ptr, [o.data_ptr() for o in out],
+                              dt, flag, mode="exact")
+    out_s = [torch.zeros(n, dtype=torch.float64, device="cuda")
+             for _ in range(6)]
+    kp.sakura_queue(n, ptr, n, ptr, [o.data_ptr() for o in out_s], dt, flag,
+                    mode="split")
+    torch.cuda.synchronize()
+    # the branch test in FP32 may flip a pair sitting on the threshold
+    assert abs(nk_s - nk_e) <= max(2, nk_e // 200)
+    want = oracle.run("sakura_kernel", ps, ps, {"dt": dt, "flag": flag})
+    for c in range(6):
+        g = out_s[c].cpu().numpy()
+        scale = np.abs(want[c]).max()
+        assert np.all(np.isfinite(g))
+        assert np.max(np.abs(g - want[c])) <= 1e-5 * scale, c
+
+
+def test_device_sakura_split_integrator_close_to_exact():
+    pytest.importorskip("torch")
+    ps = ics.plummer(512, eps=0.0, seed=17, masses="salpeter")
+    tau, t_end = 1.0 / 256, 1.0 / 32
+    res = {}
+    for mode in ("exact", "split"):
+        dev = kp.DeviceSakura(ps, mode=mode)
+        dev.evolve(tau, t_end)
+        res[mode] = dev.state()
+        dev.close()
+    for k in ("rx", "ry", "rz", "vx", "vy", "vz"):
+        e, s = res["exact"][k], res["split"][k]
+        assert np.abs(e - s).max() <= 1e-7 * np.abs(e).max(), k

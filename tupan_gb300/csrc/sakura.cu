@@ -29,10 +29,14 @@
 
 #include "tg_common.cuh"
 #include "tg_kepler.cuh"
+#include "tg_split_ops.cuh"
 
 #define TG_EXPORT extern "C" __attribute__((visibility("default")))
 
 namespace tg {
+
+cudaError_t launch_pack(int kernel, uint64_t n, const void *const *attrs,
+                        float4 *out, cudaStream_t st);
 
 // ---------------------------------------------------------------------------
 // Learned start: parameters in device memory.
@@ -289,6 +293,94 @@ k_sakura_pass(const SakuraArgs A)
     }
 }
 
+// SPLIT mode of the two passes (flags -1 and +1): FP32 pair arithmetic on
+// the packed double-single records.  In the leapfrog branch the pair's
+// change over the step has a closed form: with the midpoint position
+// b = r0 + flag v0 dt/2 and a = -m b / |b|^3 (softened), the velocity
+// changes by a dt and the position by -flag a dt^2/2 (the algebra of
+// sakura_kernel_common.h:45-91 with :151-164), so each pair is one
+// acceleration evaluation formed directly as increments (no difference of
+// nearly equal FP32 states).  The branch test is the reference's
+// (r^2 > (64 m / v^2)^2, sakura_kernel_common.h:109-123) in FP32; both
+// passes take the same decisions.  Kepler-branch pairs go to the same
+// queue and fp64 solver as in EXACT mode.
+constexpr int SKS_TILE = 256;
+
+template <int PASS>
+__global__ void __launch_bounds__(SK_THREADS)
+k_sakura_split_pass(const SakuraArgs A, const float4 *irec, const float4 *jrec)
+{
+    __shared__ float4 tile[SKS_TILE * 3];
+    const uint64_t i = (uint64_t)blockIdx.x * SK_THREADS + threadIdx.x;
+    const uint64_t ic = i < A.ni ? i : A.ni - 1;
+    const float4 ia = irec[3 * ic], ib = irec[3 * ic + 1], iv = irec[3 * ic + 2];
+    const float fl = (float)A.flag;
+    const float dt = (float)A.dt, hdt = 0.5f * dt, dt2h = 0.5f * dt * dt;
+    double o[6] = {0, 0, 0, 0, 0, 0};
+    float part[6] = {0, 0, 0, 0, 0, 0};
+    int run = 0;
+    unsigned count = 0;
+    const unsigned base = (PASS == 2 && i < A.ni) ? A.cnt[i] : 0;
+    for (uint64_t j0 = 0; j0 < A.nj; j0 += SKS_TILE) {
+        const int n = (int)((A.nj - j0) < SKS_TILE ? (A.nj - j0) : SKS_TILE);
+        __syncthreads();
+        for (int t = threadIdx.x; t < 3 * n; t += SK_THREADS)
+            tile[t] = jrec[3 * j0 + t];
+        __syncthreads();
+        for (int jj = 0; jj < n; ++jj) {
+            const float4 ja = tile[3 * jj], jb = tile[3 * jj + 1],
+                         jv = tile[3 * jj + 2];
+            const float dx = (ia.x - ja.x) + (ib.x - jb.x);
+            const float dy = (ia.y - ja.y) + (ib.y - jb.y);
+            const float dz = (ia.z - ja.z) + (ib.z - jb.z);
+            const float ux = iv.x - jv.x, uy = iv.y - jv.y, uz = iv.z - jv.z;
+            const float m = ia.w + ja.w, e2 = ib.w + jb.w;
+            // state the two-body step starts from: flag -1 drifts back first
+            const float sh = fl < 0.f ? -dt : 0.f;
+            const float px = fmaf(ux, sh, dx), py = fmaf(uy, sh, dy),
+                        pz = fmaf(uz, sh, dz);
+            const float r2p = fmaf(pz, pz, fmaf(py, py, px * px));
+            const float v2 = fmaf(uz, uz, fmaf(uy, uy, ux * ux));
+            const float R = 64.0f * (m / v2);
+            if (!(r2p > R * R)) {           // Kepler branch
+                if (PASS == 2 && i < A.ni) {
+                    A.queue_j[base + count] = (unsigned)(j0 + jj);
+                    A.queue_i[base + count] = (unsigned)i;
+                }
+                ++count;
+                continue;
+            }
+            if (PASS == 1) continue;
+            const float bx = fmaf(ux, fl * hdt, dx), by = fmaf(uy, fl * hdt, dy),
+                        bz = fmaf(uz, fl * hdt, dz);
+            const float r2b = fmaf(bz, bz, fmaf(by, by, bx * bx));
+            float y = rsqrt_nr(r2b + e2);
+            y = r2b > 0.f ? y : 0.f;
+            const float jmk = -ja.w * (y * y) * y;      // -(m_j/m) m k
+            const float av = jmk * dt, ar = -fl * jmk * dt2h;
+            part[0] = fmaf(ar, bx, part[0]);
+            part[1] = fmaf(ar, by, part[1]);
+            part[2] = fmaf(ar, bz, part[2]);
+            part[3] = fmaf(av, bx, part[3]);
+            part[4] = fmaf(av, by, part[4]);
+            part[5] = fmaf(av, bz, part[5]);
+            if (++run == 16) {
+                for (int q = 0; q < 6; ++q) {
+                    o[q] += (double)part[q];
+                    part[q] = 0.f;
+                }
+                run = 0;
+            }
+        }
+    }
+    if (i >= A.ni) return;
+    if (PASS == 1) {
+        A.cnt[i] = count;
+    } else {
+        for (int q = 0; q < 6; ++q) A.out[q][i] = o[q] + (double)part[q];
+    }
+}
+
 // Exclusive scan of n counts in place (one block; returns the total).
 __global__ void k_scan(unsigned *x, uint64_t n, unsigned long long *total)
 {
@@ -385,6 +477,8 @@ struct SakuraWork {
     size_t q_cap = 0;
     unsigned long long *total = nullptr;
     unsigned *err = nullptr;
+    float4 *rec = nullptr;            // SPLIT mode: packed i and j records
+    size_t rec_cap = 0;
 };
 
 SakuraWork g_work;
@@ -496,9 +590,10 @@ TG_EXPORT int tupan_gb300_sakura_queue(uint64_t ni, const void *const *i_attrs,
                                        void *const *outs, int use_mlp,
                                        long long budget, void *stream,
                                        unsigned long long *n_kepler,
-                                       long long *kepler_iters)
+                                       long long *kepler_iters, int mode)
 {
     if (flag != -1 && flag != 1) return ST_BAD_ARGUMENT;
+    if (mode != MODE_EXACT && mode != MODE_SPLIT) return ST_BAD_ARGUMENT;
     if (use_mlp && !g_have_mlp) return ST_BAD_ARGUMENT;
     if (ni == 0) return ST_OK;
     cudaStream_t st = (cudaStream_t)stream;
@@ -532,7 +627,32 @@ TG_EXPORT int tupan_gb300_sakura_queue(uint64_t ni, const void *const *i_attrs,
     A.mlp = g_mlp;
     cudaMemsetAsync(g_work.err, 0, sizeof(unsigned), st);
     const unsigned blocks = (unsigned)((ni + SK_THREADS - 1) / SK_THREADS);
-    k_sakura_pass<1><<<blocks, SK_THREADS, 0, st>>>(A);
+    const float4 *irec = nullptr, *jrec = nullptr;
+    if (mode == MODE_SPLIT) {
+        bool same = ni == nj;
+        for (int a = 0; a < 8 && same; ++a) same = i_attrs[a] == j_attrs[a];
+        const size_t need = (ni + (same ? 0 : nj)) * 3;
+        if (need > g_work.rec_cap) {
+            cudaFree(g_work.rec);
+            g_work.rec = nullptr;
+            g_work.rec_cap = 0;
+            if (cudaMalloc((void **)&g_work.rec, need * sizeof(float4)) !=
+                cudaSuccess)
+                return ST_CUDA;
+            g_work.rec_cap = need;
+        }
+        if (launch_pack(K_ACC_JERK, ni, i_attrs, g_work.rec, st) != cudaSuccess)
+            return ST_CUDA;
+        if (!same && launch_pack(K_ACC_JERK, nj, j_attrs, g_work.rec + ni * 3,
+                                 st) != cudaSuccess)
+            return ST_CUDA;
+        irec = g_work.rec;
+        jrec = same ? g_work.rec : g_work.rec + ni * 3;
+    }
+    if (mode == MODE_SPLIT)
+        k_sakura_split_pass<1><<<blocks, SK_THREADS, 0, st>>>(A, irec, jrec);
+    else
+        k_sakura_pass<1><<<blocks, SK_THREADS, 0, st>>>(A);
     k_scan<<<1, 1024, 0, st>>>(g_work.cnt, ni, g_work.total);
     g_launch_count += 2;
     unsigned long long nq = 0;
@@ -545,7 +665,10 @@ TG_EXPORT int tupan_gb300_sakura_queue(uint64_t ni, const void *const *i_attrs,
     A.queue_j = g_work.qj;
     A.contrib = g_work.contrib;
     A.iters = kepler_iters ? g_work.iters : nullptr;
-    k_sakura_pass<2><<<blocks, SK_THREADS, 0, st>>>(A);
+    if (mode == MODE_SPLIT)
+        k_sakura_split_pass<2><<<blocks, SK_THREADS, 0, st>>>(A, irec, jrec);
+    else
+        k_sakura_pass<2><<<blocks, SK_THREADS, 0, st>>>(A);
     g_launch_count += 1;
     if (nq) {
         k_sakura_kepler<<<(unsigned)((nq + 127) / 128), 128, 0, st>>>(
@@ -607,6 +730,7 @@ struct SakuraSys {
     double **xd = nullptr, **dd = nullptr;   // device arrays of pointers
     cudaStream_t stream = nullptr;
     int use_mlp = 0;
+    int mode = MODE_EXACT;           // Sakura sweeps: EXACT or SPLIT
     long long kepler_total = 0, steps = 0;
     long long hist[65] = {0};
     double t = 0.0;
@@ -673,7 +797,8 @@ TG_EXPORT int tupan_gb300_sakura_evolve(void *handle, double tau, double t_end,
             unsigned long long nk = 0;
             int st = tupan_gb300_sakura_queue(n, ia, n, ia, tau / 2, flag, oa,
                                               use_mlp, 0, S->stream, &nk,
-                                              kepler_iters ? h : nullptr);
+                                              kepler_iters ? h : nullptr,
+                                              S->mode);
             if (st) return st;
             S->kepler_total += (long long)nk;
             if (kepler_iters)
@@ -691,6 +816,15 @@ TG_EXPORT int tupan_gb300_sakura_evolve(void *handle, double tau, double t_end,
     if (t_out) *t_out = S->t;
     if (steps_out) *steps_out = S->steps;
     if (kepler_out) *kepler_out = S->kepler_total;
+    return ST_OK;
+}
+
+// Sakura sweeps of the integrator: mode 0 EXACT (default), 1 SPLIT.
+TG_EXPORT int tupan_gb300_sakura_set_mode(void *handle, int mode)
+{
+    SakuraSys *S = (SakuraSys *)handle;
+    if (!S || (mode != MODE_EXACT && mode != MODE_SPLIT)) return ST_BAD_ARGUMENT;
+    S->mode = mode;
     return ST_OK;
 }
 

@@ -21,7 +21,7 @@ def _declare(L):
     L.tupan_gb300_sakura_queue.argtypes = [
         c.c_uint64, c.POINTER(_VP), c.c_uint64, c.POINTER(_VP), c.c_double,
         c.c_int64, c.POINTER(_VP), c.c_int, c.c_longlong, _VP,
-        c.POINTER(c.c_ulonglong), c.POINTER(c.c_longlong)]
+        c.POINTER(c.c_ulonglong), c.POINTER(c.c_longlong), c.c_int]
     L.tupan_gb300_sakura_queue.restype = c.c_int
 
 
@@ -38,9 +38,11 @@ def _ptr(t):
 
 
 def sakura_queue(ni, i_ptrs, nj, j_ptrs, out_ptrs, dt, flag, use_mlp=False,
-                 budget=0, stream=None, histogram=False):
+                 budget=0, stream=None, histogram=False, mode="exact"):
     """sakura_kernel over device arrays (flag -1 or +1).  Returns the number
-    of Kepler-branch pairs and, if asked, the Laguerre-update histogram."""
+    of Kepler-branch pairs and, if asked, the Laguerre-update histogram.
+    mode "split": leapfrog-branch pairs in FP32 on double-single positions
+    (the Kepler branch stays fp64)."""
     L = _lib()
     ia = (_VP * 8)(*i_ptrs)
     ja = (_VP * 8)(*j_ptrs)
@@ -50,7 +52,8 @@ def sakura_queue(ni, i_ptrs, nj, j_ptrs, out_ptrs, dt, flag, use_mlp=False,
     st = L.tupan_gb300_sakura_queue(int(ni), ia, int(nj), ja, float(dt),
                                     int(flag), oa, 1 if use_mlp else 0,
                                     int(budget), stream, ctypes.byref(nk),
-                                    hist)
+                                    hist, lib.MODE_SPLIT if mode == "split"
+                                    else lib.MODE_EXACT)
     if st:
         raise lib.TupanGB300Error("sakura_queue failed: status %d" % st)
     return nk.value, (np.array(hist[:]) if histogram else None)
@@ -91,9 +94,11 @@ class DeviceSakura(object):
 
     KEYS = ("m", "e2", "rx", "ry", "rz", "vx", "vy", "vz")
 
-    def __init__(self, ps):
+    def __init__(self, ps, mode="exact"):
         L = _lib()
         c = ctypes
+        L.tupan_gb300_sakura_set_mode.argtypes = [_VP, c.c_int]
+        L.tupan_gb300_sakura_set_mode.restype = c.c_int
         L.tupan_gb300_sakura_create.argtypes = [c.c_uint64] + [_DP] * 8 + [
             c.POINTER(_VP)]
         L.tupan_gb300_sakura_create.restype = c.c_int
@@ -118,6 +123,10 @@ class DeviceSakura(object):
             raise lib.TupanGB300Error("sakura_create failed: status %d" % st)
         self.h = h
         self.hist = np.zeros(65, np.int64)
+        if mode != "exact":
+            if L.tupan_gb300_sakura_set_mode(
+                    h, lib.MODE_SPLIT if mode == "split" else -1):
+                raise ValueError("unexpected mode: %r" % (mode,))
 
     def evolve(self, tau, t_end, use_mlp=False):
         t = ctypes.c_double()

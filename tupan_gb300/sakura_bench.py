@@ -19,10 +19,11 @@ import numpy as np
 
 def integrate(a):
     """The Sakura integrator on the device (N = a.n Salpeter Plummer sphere,
-    eps = 0, fixed step tau to t_end), once with the plain Kepler start and
-    once with the learned start: wall time, Kepler solves and their rate,
-    mean Laguerre updates, and the largest difference between the two final
-    states relative to the coordinate scale."""
+    eps = 0, fixed step tau to t_end): EXACT sweeps with the plain Kepler
+    start, EXACT with the learned start, and SPLIT sweeps.  Wall time,
+    Kepler solves and their rate, mean Laguerre updates, and the largest
+    difference of each final state from the first, relative to the
+    coordinate scale."""
     import time
     import torch
     from . import ics, learned
@@ -31,10 +32,15 @@ def integrate(a):
     res = {"n": a.n, "tau": a.tau, "t_end": a.t_end}
     finals = {}
     net = learned.LearnedStart.load(a.weights or learned.WEIGHTS)
-    for label, use in (("plain", False), ("learned", True)):
+    runs = (("plain", False, "exact"), ("learned", True, "exact"),
+            ("split", False, "split"))
+    for label, use, mode in runs:
         if use:
             net.install()
-        d = DeviceSakura(ps)
+        else:
+            from .kepler import clear_mlp
+            clear_mlp()
+        d = DeviceSakura(ps, mode=mode)
         torch.cuda.synchronize()
         t0 = time.perf_counter()
         t, steps, nk = d.evolve(a.tau, a.t_end, use_mlp=use)
@@ -49,12 +55,15 @@ def integrate(a):
                                             max(h.sum(), 1))}
     from .kepler import clear_mlp
     clear_mlp()
-    diff = 0.0
-    for c in ("rx", "ry", "rz", "vx", "vy", "vz"):
-        scale = np.abs(finals["plain"][c]).max()
-        diff = max(diff, float(np.abs(finals["plain"][c] -
-                                      finals["learned"][c]).max() / scale))
-    res["max_state_diff_over_scale"] = diff
+    for other in ("learned", "split"):
+        diff = 0.0
+        for c in ("rx", "ry", "rz", "vx", "vy", "vz"):
+            scale = np.abs(finals["plain"][c]).max()
+            diff = max(diff, float(np.abs(finals["plain"][c] -
+                                          finals[other][c]).max() / scale))
+        res["max_state_diff_over_scale_" + other] = diff
+    res["split_over_plain_wall"] = (res["plain"]["wall_s"] /
+                                    res["split"]["wall_s"])
     res["learned_over_plain_wall"] = (res["plain"]["wall_s"] /
                                       res["learned"]["wall_s"])
     print(json.dumps(res))
@@ -109,6 +118,9 @@ def main(argv=None):
                                histogram=True)
     t_queue = timed(lambda: kp.sakura_queue(n, ptr, n, ptr, optr, a.dt, -1))
     res["queue_pairs_per_s"] = n * n / t_queue
+    t_split = timed(lambda: kp.sakura_queue(n, ptr, n, ptr, optr, a.dt, -1,
+                                            mode="split"))
+    res["queue_split_pairs_per_s"] = n * n / t_split
     res["kepler_pairs"] = int(nk)
     res["hist_plain"] = hist[:12].tolist()
     res["mean_iters_plain"] = float((np.arange(65) * hist).sum() / max(nk, 1))
