@@ -440,7 +440,8 @@ def main():
                     "fp64_sample_ni": ni64,
                     "split_over_fp64": (inter / t_step) / (2.0 * ni64 * n / t64),
                     "acc_rel_err_vs_fp64_oracle": acc_err},
-        "roofline": {"bound": "fp32", "kernel": "split_sweep<AccJerkS>",
+        "roofline": {"bound": "fp32",
+                     "kernel": "split_sweep<AccJerkS> variant %d" % v_aj,
                      "achieved": achieved, "peak": fp32_peak,
                      "unit": "TFLOP/s", "frac": achieved / fp32_peak,
                      "flops_per_interaction": FLOPS_ACC_JERK,

@@ -253,7 +253,7 @@ def test_split_phi_tstep_snap_accuracy():
         np.median(es), np.median(ec))
 
 
-@pytest.mark.parametrize("variant", range(9))
+@pytest.mark.parametrize("variant", range(12))
 @pytest.mark.parametrize("gsplit", [1, 3, 8])
 def test_split_every_variant(variant, gsplit):
     ps = ics.plummer(3000, eps=1e-4, seed=5)
@@ -265,10 +265,41 @@ def test_split_every_variant(variant, gsplit):
     finally:
         lib.set_split_config("acc_jerk_kernel", -1, 0)
     ea = vec_rel_err(got, want, (0, 1, 2))
+    ej = vec_rel_err(got, want, (3, 4, 5))
     assert ea.max() <= 1e-6, ea.max()
+    assert np.median(ej) <= 1e-6 and ej.max() <= 1e-4, (ej.max(),
+                                                        np.median(ej))
 
 
-@pytest.mark.parametrize("variant", range(7))
+@pytest.mark.parametrize("variant", [9, 10, 11])
+@pytest.mark.parametrize("name", ["phi_kernel", "acc_kernel"])
+def test_split_no_newton_variants(name, variant):
+    # 1/sqrt from the MUFU approximation alone: the same |da|/|a| and
+    # |dphi|/|phi| <= 1e-6 bound as the Newton-step forms
+    ps = ics.plummer(4000, eps=1e-4, seed=25)
+    js = {k: np.ascontiguousarray(v[:3700]) for k, v in ps.items()}
+    want = oracle.run(name, ps, js)
+    lib.set_split_config(name, variant, 2)
+    try:
+        got = run_gpu(name, ps, js, mode=lib.MODE_SPLIT)
+    finally:
+        lib.set_split_config(name, -1, 0)
+    if name == "phi_kernel":
+        err = np.abs(got[0] - want[0]) / np.abs(want[0])
+    else:
+        err = vec_rel_err(got, want, (0, 1, 2))
+    assert err.max() <= 1e-6, (err.max(), np.median(err))
+
+
+def test_split_model_prefers_no_newton_forms():
+    for name in ("phi_kernel", "acc_kernel", "acc_jerk_kernel"):
+        v, g = lib.split_choice(name, 262144, 262144)
+        assert v in (9, 11), (name, v, g)
+    v, g = lib.split_choice("tstep_kernel", 262144, 262144)
+    assert v not in (9, 10, 11), v
+
+
+@pytest.mark.parametrize("variant", range(12))
 @pytest.mark.parametrize("gsplit", [1, 3])
 def test_split_tstep_every_variant(variant, gsplit):
     # variants 5 and 6 evaluate two i per thread as packed FP32 pairs
@@ -286,7 +317,7 @@ def test_split_tstep_every_variant(variant, gsplit):
         assert np.max(np.abs(g - w) / w) <= 1e-5
 
 
-@pytest.mark.parametrize("variant", range(7))
+@pytest.mark.parametrize("variant", range(12))
 @pytest.mark.parametrize("gsplit", [1, 3])
 def test_split_snap_crackle_every_variant(variant, gsplit):
     ps = ics.plummer(2500, eps=1e-4, seed=16)

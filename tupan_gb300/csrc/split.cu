@@ -106,7 +106,9 @@ split_sweep(const SplitLaunch L)
     constexpr int NJF = NF;                   // float4 per j-record
     constexpr int TJ = SPLIT_TILE;
     // Records per lane summed in FP32 before a Kahan fold: short runs keep
-    // the FP32 rounding of each run small next to the particle's |a|.
+    // the FP32 rounding of each run small next to the particle's |a|
+    // (runs of 32 measured max |da|/|a| 1.09e-6 at N = 3000; 16 stay
+    // inside 1e-6).
     constexpr int FOLD = (TJ / JS) < 16 ? (TJ / JS) : 16;
     static_assert(TJ % (JS * FOLD) == 0, "fold must divide the tile");
     constexpr int GROUPS = NT / JS;          // i-groups per CTA
@@ -184,41 +186,68 @@ split_sweep(const SplitLaunch L)
 #pragma unroll
             for (int q = 0; q < NP; ++q)
                 ip2[q] = OpX2::pack(ip[2 * q], ip[2 * q + 1]);
+            auto run_tile = [&](auto pairfn) {
 #pragma unroll 1
-            for (int r0 = js; r0 < n; r0 += JS * FOLD) {
-                float2 p2[NP][NO];
+                for (int r0 = js; r0 < n; r0 += JS * FOLD) {
+                    float2 p2[NP][NO];
 #pragma unroll
-                for (int q = 0; q < NP; ++q)
+                    for (int q = 0; q < NP; ++q)
 #pragma unroll
-                    for (int c = 0; c < NO; ++c) p2[q][c] = make_float2(0.f, 0.f);
-                if (n == TJ) {
+                        for (int c = 0; c < NO; ++c)
+                            p2[q][c] = make_float2(0.f, 0.f);
+                    if (n == TJ) {
 #pragma unroll
-                    for (int u = 0; u < FOLD; ++u) {
-                        const typename Op::P jp =
-                            Op::load(tile + (r0 + u * JS) * NF);
+                        for (int u = 0; u < FOLD; ++u) {
+                            const typename Op::P jp =
+                                Op::load(tile + (r0 + u * JS) * NF);
 #pragma unroll
-                        for (int q = 0; q < NP; ++q)
-                            OpX2::pair(ip2[q], jp, p2[q], L.eta);
-                    }
-                } else {
+                            for (int q = 0; q < NP; ++q) pairfn(q, jp, p2[q]);
+                        }
+                    } else {
 #pragma unroll 1
-                    for (int u = 0; u < FOLD && r0 + u * JS < n; ++u) {
-                        const typename Op::P jp =
-                            Op::load(tile + (r0 + u * JS) * NF);
+                        for (int u = 0; u < FOLD && r0 + u * JS < n; ++u) {
+                            const typename Op::P jp =
+                                Op::load(tile + (r0 + u * JS) * NF);
 #pragma unroll
-                        for (int q = 0; q < NP; ++q)
-                            OpX2::pair(ip2[q], jp, p2[q], L.eta);
+                            for (int q = 0; q < NP; ++q) pairfn(q, jp, p2[q]);
+                        }
                     }
+#pragma unroll
+                    for (int q = 0; q < NP; ++q)
+#pragma unroll
+                        for (int c = 0; c < NO; ++c) {
+                            part[(2 * q) % NI][c] = p2[q][c].x;
+                            part[(2 * q + 1) % NI][c] = p2[q][c].y;
+                        }
+                    fold();
                 }
-#pragma unroll
-                for (int q = 0; q < NP; ++q)
-#pragma unroll
-                    for (int c = 0; c < NO; ++c) {
-                        part[(2 * q) % NI][c] = p2[q][c].x;
-                        part[(2 * q + 1) % NI][c] = p2[q][c].y;
-                    }
-                fold();
+            };
+            bool uniform = false;
+            float e2t = 0.f;
+            if constexpr (OpX2::HAS_H2) {
+                // One softening for every record of the tile (the common
+                // case): h2 = e2_i + e2_tile is formed once per tile.
+                e2t = tile[1].w;
+                bool same = true;
+                for (int r = tid; r < n; r += NT)
+                    same = same && (tile[r * NF + 1].w == e2t);
+                uniform = __syncthreads_and(same);
             }
+            if constexpr (OpX2::HAS_H2) {
+                if (uniform) {
+                    float2 h2t[NP];
+#pragma unroll
+                    for (int q = 0; q < NP; ++q)
+                        h2t[q] = add2(ip2[q].e2, dup(e2t));
+                    run_tile([&](int q, const typename Op::P &jp, float2 *a) {
+                        OpX2::pair_h2(ip2[q], jp, a, h2t[q]);
+                    });
+                }
+            }
+            if (!uniform)
+                run_tile([&](int q, const typename Op::P &jp, float2 *a) {
+                    OpX2::pair(ip2[q], jp, a, L.eta);
+                });
         } else if (n == TJ) {
 #pragma unroll 1
             for (int r0 = 0; r0 < TJ; r0 += JS * FOLD) {
@@ -325,6 +354,9 @@ static const VariantInfo kVariants[] = {
     {2, 4, 256},   // packed, lanes split the j-tile
     {4, 1, 256},   // packed, two pairs per thread (one CTA per SM)
     {2, 1, 256},   // as 5 with the registers of one CTA per SM
+    {2, 1, 256},   // as 5, 1/sqrt without the Newton step
+    {4, 1, 256},   // as 7, 1/sqrt without the Newton step
+    {2, 1, 256},   // as 0, 1/sqrt without the Newton step
 };
 constexpr int N_VARIANTS = sizeof(kVariants) / sizeof(kVariants[0]);
 
@@ -337,7 +369,20 @@ void split_variant_info(int v, int *ni_per_thread, int *jsplit, int *threads)
     *threads = kVariants[v].threads;
 }
 
-// Kernels with a packed-pair (f32x2) operator: variants 5 to 8 use it.
+// Variants 9 to 11 take 1/sqrt from the MUFU approximation alone; the
+// operators with that form are Phi, Acc and AccJerk (others run their
+// Newton-step form under those numbers).
+template <class Op> struct RawOf { using type = Op; };
+template <> struct RawOf<PhiS> { using type = PhiSN<false>; };
+template <> struct RawOf<AccS> { using type = AccSN<false>; };
+template <> struct RawOf<AccJerkS> { using type = AccJerkSN<false>; };
+
+bool split_has_raw(int kernel)
+{
+    return kernel == K_PHI || kernel == K_ACC || kernel == K_ACC_JERK;
+}
+
+// Kernels with a packed-pair (f32x2) operator: variants 5 to 10 use it.
 bool split_has_x2(int kernel)
 {
     return kernel == K_PHI || kernel == K_ACC || kernel == K_ACC_JERK ||
@@ -395,6 +440,16 @@ static cudaError_t run_op(const SplitLaunch &L, int variant, int gsplit,
         } else {
             return run_variant<Op, 2, 1, 256, 2>(L, gsplit, st);
         }
+    case 9:
+    case 10:
+    case 11: {
+        using R = typename RawOf<Op>::type;
+        if constexpr (!std::is_void<typename X2Of<R>::type>::value) {
+            if (variant == 9) return run_variant<R, 2, 1, 256, 2, true>(L, gsplit, st);
+            if (variant == 10) return run_variant<R, 4, 1, 256, 1, true>(L, gsplit, st);
+        }
+        return run_variant<R, 2, 1, 256, 2>(L, gsplit, st);
+    }
     default: return cudaErrorInvalidValue;
     }
 }

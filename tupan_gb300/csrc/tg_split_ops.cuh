@@ -33,9 +33,25 @@ __device__ __forceinline__ float rsqrt_nr(float s)
     return fmaf(0.5f * y, e, y);
 }
 
-struct PhiS {
+// 1/sqrt(s): with the Newton step (NR) or the MUFU approximation alone
+// (relative error about 2^-23 per pair, which the sums of many pairs keep
+// well inside the sweep's |da|/|a| <= 1e-6 bound; four FP32 operations less).
+template <bool NR>
+__device__ __forceinline__ float rsq(float s)
+{
+    if constexpr (NR) return rsqrt_nr(s);
+    else return rsqrtf(s);
+}
+
+// Register images of a packed record: position (+ mass, softening) and
+// position-velocity.
+struct PosRec { float xh, yh, zh, m, xl, yl, zl, e2; };
+struct PosVelRec { float xh, yh, zh, m, xl, yl, zl, e2, vx, vy, vz; };
+
+template <bool NR>
+struct PhiSN {
     static constexpr int NF = 2, NO = 1, MAXC = -1;
-    struct P { float xh, yh, zh, m, xl, yl, zl, e2; };
+    using P = PosRec;
     __device__ static P load(const float4 *r)
     {
         float4 a = r[0], b = r[1];
@@ -48,14 +64,16 @@ struct PhiS {
         float dz = (j.zh - i.zh) + (j.zl - i.zl);
         float h2 = i.e2 + j.e2;
         float s = fmaf(dz, dz, fmaf(dy, dy, fmaf(dx, dx, h2)));
-        float y = rsqrt_nr(s);
+        float y = rsq<NR>(s);
         y = (s > h2) ? y : 0.0f;
         acc[0] = fmaf(-j.m, y, acc[0]);
     }
     __device__ static void finish(double *, double) {}
 };
+using PhiS = PhiSN<true>;
 
-struct AccS {
+template <bool NR>
+struct AccSN {
     static constexpr int NF = 2, NO = 3, MAXC = -1;
     using P = PhiS::P;
     __device__ static P load(const float4 *r) { return PhiS::load(r); }
@@ -66,7 +84,7 @@ struct AccS {
         float dz = (j.zh - i.zh) + (j.zl - i.zl);
         float h2 = i.e2 + j.e2;
         float s = fmaf(dz, dz, fmaf(dy, dy, fmaf(dx, dx, h2)));
-        float y = rsqrt_nr(s);
+        float y = rsq<NR>(s);
         y = (s > h2) ? y : 0.0f;
         float mk = (j.m * y) * (y * y);
         acc[0] = fmaf(mk, dx, acc[0]);
@@ -75,10 +93,12 @@ struct AccS {
     }
     __device__ static void finish(double *, double) {}
 };
+using AccS = AccSN<true>;
 
-struct AccJerkS {
+template <bool NR>
+struct AccJerkSN {
     static constexpr int NF = 3, NO = 6, MAXC = -1;
-    struct P { float xh, yh, zh, m, xl, yl, zl, e2, vx, vy, vz; };
+    using P = PosVelRec;
     __device__ static P load(const float4 *r)
     {
         float4 a = r[0], b = r[1], c = r[2];
@@ -93,7 +113,7 @@ struct AccJerkS {
         float h2 = i.e2 + j.e2;
         float s = fmaf(dz, dz, fmaf(dy, dy, fmaf(dx, dx, h2)));
         float rv = fmaf(dz, uz, fmaf(dy, uy, dx * ux));
-        float y = rsqrt_nr(s);
+        float y = rsq<NR>(s);
         y = (s > h2) ? y : 0.0f;
         float y2 = y * y;
         float mk = (j.m * y) * y2;
@@ -107,6 +127,7 @@ struct AccJerkS {
     }
     __device__ static void finish(double *, double) {}
 };
+using AccJerkS = AccJerkSN<true>;
 
 // tstep_kernel_common.h:7-60 in FP32; output 0 sums w2, output 1 is max w2.
 struct TstepS {
@@ -238,7 +259,18 @@ __device__ __forceinline__ float2 rsqrt_nr2(float2 s, float2 h2)
     return y;
 }
 
-struct PhiS2 {
+template <bool NR>
+__device__ __forceinline__ float2 rsq2(float2 s, float2 h2)
+{
+    if constexpr (NR) return rsqrt_nr2(s, h2);
+    float2 y = make_float2(rsqrtf(s.x), rsqrtf(s.y));
+    y.x = (s.x > h2.x) ? y.x : 0.0f;
+    y.y = (s.y > h2.y) ? y.y : 0.0f;
+    return y;
+}
+
+template <bool NR>
+struct PhiS2N {
     using P = PhiS::P;
     using I = PosI2;
     __device__ static I pack(const P &a, const P &b)
@@ -248,38 +280,52 @@ struct PhiS2 {
                 make_float2(-a.yl, -b.yl), make_float2(-a.zl, -b.zl),
                 make_float2(a.e2, b.e2)};
     }
-    __device__ static void pair(const I &i, const P &j, float2 *acc, float)
+    static constexpr bool HAS_H2 = true;
+    // h2 = e2_i + e2_j given (formed once per tile when the tile's records
+    // share one softening)
+    __device__ static void pair_h2(const I &i, const P &j, float2 *acc,
+                                   float2 h2)
     {
         float2 dx = add2(add2(dup(j.xh), i.nxh), add2(dup(j.xl), i.nxl));
         float2 dy = add2(add2(dup(j.yh), i.nyh), add2(dup(j.yl), i.nyl));
         float2 dz = add2(add2(dup(j.zh), i.nzh), add2(dup(j.zl), i.nzl));
-        float2 h2 = add2(i.e2, dup(j.e2));
         float2 s = fma2(dz, dz, fma2(dy, dy, fma2(dx, dx, h2)));
-        float2 y = rsqrt_nr2(s, h2);
+        float2 y = rsq2<NR>(s, h2);
         acc[0] = fma2(dup(-j.m), y, acc[0]);
+    }
+    __device__ static void pair(const I &i, const P &j, float2 *acc, float)
+    {
+        pair_h2(i, j, acc, add2(i.e2, dup(j.e2)));
     }
 };
 
-struct AccS2 {
+template <bool NR>
+struct AccS2N {
     using P = PhiS::P;
     using I = PosI2;
-    __device__ static I pack(const P &a, const P &b) { return PhiS2::pack(a, b); }
-    __device__ static void pair(const I &i, const P &j, float2 *acc, float)
+    __device__ static I pack(const P &a, const P &b) { return PhiS2N<NR>::pack(a, b); }
+    static constexpr bool HAS_H2 = true;
+    __device__ static void pair_h2(const I &i, const P &j, float2 *acc,
+                                   float2 h2)
     {
         float2 dx = add2(add2(dup(j.xh), i.nxh), add2(dup(j.xl), i.nxl));
         float2 dy = add2(add2(dup(j.yh), i.nyh), add2(dup(j.yl), i.nyl));
         float2 dz = add2(add2(dup(j.zh), i.nzh), add2(dup(j.zl), i.nzl));
-        float2 h2 = add2(i.e2, dup(j.e2));
         float2 s = fma2(dz, dz, fma2(dy, dy, fma2(dx, dx, h2)));
-        float2 y = rsqrt_nr2(s, h2);
+        float2 y = rsq2<NR>(s, h2);
         float2 mk = mul2(mul2(dup(j.m), y), mul2(y, y));
         acc[0] = fma2(mk, dx, acc[0]);
         acc[1] = fma2(mk, dy, acc[1]);
         acc[2] = fma2(mk, dz, acc[2]);
     }
+    __device__ static void pair(const I &i, const P &j, float2 *acc, float)
+    {
+        pair_h2(i, j, acc, add2(i.e2, dup(j.e2)));
+    }
 };
 
-struct AccJerkS2 {
+template <bool NR>
+struct AccJerkS2N {
     using P = AccJerkS::P;
     using I = PosVelI2;
     __device__ static I pack(const P &a, const P &b)
@@ -290,7 +336,13 @@ struct AccJerkS2 {
                 make_float2(a.e2, b.e2),   make_float2(-a.vx, -b.vx),
                 make_float2(-a.vy, -b.vy), make_float2(-a.vz, -b.vz)};
     }
+    static constexpr bool HAS_H2 = true;
     __device__ static void pair(const I &i, const P &j, float2 *acc, float)
+    {
+        pair_h2(i, j, acc, add2(i.e2, dup(j.e2)));
+    }
+    __device__ static void pair_h2(const I &i, const P &j, float2 *acc,
+                                   float2 h2)
     {
         float2 dx = add2(add2(dup(j.xh), i.nxh), add2(dup(j.xl), i.nxl));
         float2 dy = add2(add2(dup(j.yh), i.nyh), add2(dup(j.yl), i.nyl));
@@ -298,10 +350,9 @@ struct AccJerkS2 {
         float2 ux = add2(dup(j.vx), i.nvx);
         float2 uy = add2(dup(j.vy), i.nvy);
         float2 uz = add2(dup(j.vz), i.nvz);
-        float2 h2 = add2(i.e2, dup(j.e2));
         float2 s = fma2(dz, dz, fma2(dy, dy, fma2(dx, dx, h2)));
         float2 rv = fma2(dz, uz, fma2(dy, uy, mul2(dx, ux)));
-        float2 y = rsqrt_nr2(s, h2);
+        float2 y = rsq2<NR>(s, h2);
         float2 y2 = mul2(y, y);
         float2 mk = mul2(mul2(dup(j.m), y), y2);
         float2 nal = mul2(mul2(rv, dup(-3.0f)), y2);
@@ -327,6 +378,7 @@ __device__ __forceinline__ float2 rsqrt_nr2_raw(float2 s)
 }
 
 struct TstepS2 {
+    static constexpr bool HAS_H2 = false;
     using P = AccJerkS::P;
     using I = PosVelMI2;
     __device__ static I pack(const P &a, const P &b)
@@ -372,6 +424,7 @@ struct SnapI2 {
 };
 
 struct SnapS2 {
+    static constexpr bool HAS_H2 = false;
     using P = SnapS::P;
     using I = SnapI2;
     __device__ static I pack(const P &a, const P &b)
@@ -446,9 +499,9 @@ struct SnapS2 {
 
 // Packed-pair partner of each scalar operator (void: none).
 template <class Op> struct X2Of { using type = void; };
-template <> struct X2Of<PhiS> { using type = PhiS2; };
-template <> struct X2Of<AccS> { using type = AccS2; };
-template <> struct X2Of<AccJerkS> { using type = AccJerkS2; };
+template <bool NR> struct X2Of<PhiSN<NR>> { using type = PhiS2N<NR>; };
+template <bool NR> struct X2Of<AccSN<NR>> { using type = AccS2N<NR>; };
+template <bool NR> struct X2Of<AccJerkSN<NR>> { using type = AccJerkS2N<NR>; };
 template <> struct X2Of<TstepS> { using type = TstepS2; };
 template <> struct X2Of<SnapS> { using type = SnapS2; };
 
