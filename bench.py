@@ -384,6 +384,43 @@ def main():
         acc_err = {"max": float(rel.max()), "median": float(np.median(rel)),
                    "sample_i": int(len(idx))}
 
+    # --- the same sweeps with the Newton step after rsqrt (the variant the
+    # default replaces: 9 -> 5, 10 -> 7, 11 -> 0), for comparison ----------
+    newton = None
+    v_def, g_def = lib.split_choice("acc_jerk_kernel", n, n)
+    v_nr = {9: 5, 10: 7, 11: 0}.get(v_def)
+    if rank == 0 and v_nr is not None:
+        for name in ("acc_kernel", "acc_jerk_kernel"):
+            lib.set_split_config(name, v_nr, g_def)
+        try:
+            step()
+            f0, f1, f2 = (torch.cuda.Event(enable_timing=True)
+                          for _ in range(3))
+            flush.fill_(0.5)
+            f0.record(stream)
+            lib.dev_sweep("acc_kernel", n, p5, n, p5,
+                          [t.data_ptr() for t in d_acc], mode=lib.MODE_SPLIT,
+                          stream=sh)
+            f1.record(stream)
+            lib.dev_sweep("acc_jerk_kernel", n, p8, n, p8,
+                          [t.data_ptr() for t in d_aj], mode=lib.MODE_SPLIT,
+                          stream=sh)
+            f2.record(stream)
+            torch.cuda.synchronize()
+        finally:
+            for name in ("acc_kernel", "acc_jerk_kernel"):
+                lib.set_split_config(name, -1, 0)
+        got = [t.cpu().numpy()[idx] for t in d_aj]
+        rel = (np.linalg.norm(np.stack(got[:3]) - wa, axis=0) /
+               np.linalg.norm(wa, axis=0))
+        newton = {"variant": v_nr, "gsplit": g_def,
+                  "acc_split_gints": n * n / (f0.elapsed_time(f1) / 1e3) / 1e9,
+                  "acc_jerk_split_gints":
+                      n * n / (f1.elapsed_time(f2) / 1e3) / 1e9,
+                  "acc_rel_err_vs_fp64_oracle": {
+                      "max": float(rel.max()),
+                      "median": float(np.median(rel))}}
+
     # --- FP64 EXACT path on an i-subset (linear in ni) ---------------------
     ni64 = min(args.fp64_ni, n)
     step(lib.MODE_EXACT, ni64)     # warm
@@ -439,7 +476,8 @@ def main():
                     "fp64_exact_acc_jerk_gints": fp64_aj_gints,
                     "fp64_sample_ni": ni64,
                     "split_over_fp64": (inter / t_step) / (2.0 * ni64 * n / t64),
-                    "acc_rel_err_vs_fp64_oracle": acc_err},
+                    "acc_rel_err_vs_fp64_oracle": acc_err,
+                    "newton_form": newton},
         "roofline": {"bound": "fp32",
                      "kernel": "split_sweep<AccJerkS> variant %d" % v_aj,
                      "achieved": achieved, "peak": fp32_peak,

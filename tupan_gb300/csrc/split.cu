@@ -159,6 +159,13 @@ split_sweep(const SplitLaunch L)
     for (int k = 0; k < NI; ++k)
 #pragma unroll
         for (int c = 0; c < NO; ++c) sum[k][c] = corr[k][c] = part[k][c] = 0.f;
+    // packed variants keep the Kahan pairs of an i pair as float2
+    float2 sum2[NP][NO], corr2[NP][NO];
+#pragma unroll
+    for (int q = 0; q < NP; ++q)
+#pragma unroll
+        for (int c = 0; c < NO; ++c)
+            sum2[q][c] = corr2[q][c] = make_float2(0.f, 0.f);
 
     auto fold = [&]() {
 #pragma unroll
@@ -212,14 +219,18 @@ split_sweep(const SplitLaunch L)
                             for (int q = 0; q < NP; ++q) pairfn(q, jp, p2[q]);
                         }
                     }
+                    // the run folds into the packed Kahan pairs of both i
 #pragma unroll
                     for (int q = 0; q < NP; ++q)
 #pragma unroll
                         for (int c = 0; c < NO; ++c) {
-                            part[(2 * q) % NI][c] = p2[q][c].x;
-                            part[(2 * q + 1) % NI][c] = p2[q][c].y;
+                            if (c == MAXC)
+                                sum2[q][c] = make_float2(
+                                    fmaxf(sum2[q][c].x, p2[q][c].x),
+                                    fmaxf(sum2[q][c].y, p2[q][c].y));
+                            else
+                                kahan_add2(sum2[q][c], corr2[q][c], p2[q][c]);
                         }
-                    fold();
                 }
             };
             bool uniform = false;
@@ -281,6 +292,18 @@ split_sweep(const SplitLaunch L)
         if (tid == 0)
             for (int s = 0; s < 2; ++s) mbar_wait_bounded(&bar[s], 0, L.err);
         return;
+    }
+
+    if constexpr (X2) {
+#pragma unroll
+        for (int q = 0; q < NP; ++q)
+#pragma unroll
+            for (int c = 0; c < NO; ++c) {
+                sum[2 * q][c] = sum2[q][c].x;
+                sum[2 * q + 1][c] = sum2[q][c].y;
+                corr[2 * q][c] = corr2[q][c].x;
+                corr[2 * q + 1][c] = corr2[q][c].y;
+            }
     }
 
     // Combine the lanes that share an i (j-split within the warp).

@@ -244,6 +244,18 @@ __device__ __forceinline__ float2 add2(float2 a, float2 b) { return __fadd2_rn(a
 __device__ __forceinline__ float2 mul2(float2 a, float2 b) { return __fmul2_rn(a, b); }
 __device__ __forceinline__ float2 fma2(float2 a, float2 b, float2 c) { return __ffma2_rn(a, b, c); }
 
+// kahan_add on both lanes, operation for operation (b - a is formed as
+// fma(a, -1, b): one rounding, the same value as the subtraction).
+__device__ __forceinline__ void kahan_add2(float2 &sum, float2 &corr,
+                                           float2 x)
+{
+    const float2 m1 = dup(-1.0f);
+    const float2 y = fma2(corr, m1, x);
+    const float2 t = add2(sum, y);
+    corr = fma2(y, m1, fma2(sum, m1, t));
+    sum = t;
+}
+
 struct PosI2 { float2 nxh, nyh, nzh, nxl, nyl, nzl, e2; };
 struct PosVelI2 { float2 nxh, nyh, nzh, nxl, nyl, nzl, e2, nvx, nvy, nvz; };
 
