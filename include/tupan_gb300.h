@@ -396,6 +396,13 @@ int tupan_gb300_ensemble_get(void *handle, double *t, long long *nsteps,
                              double *rx, double *ry, double *rz, double *vx,
                              double *vy, double *vz);
 int tupan_gb300_ensemble_destroy(void *handle);
+/* mode 0 (default): every step of every system is five batched launches.
+ * mode 1: persistent launches in which one CTA steps one whole system for up
+ * to steps_per_launch steps (records resident in shared memory, no
+ * inter-CTA waits), until fewer than switch_below systems are left, which
+ * finish in mode 0 (switch_below 0: persistent to the end). */
+int tupan_gb300_ensemble_set_mode(void *handle, int mode, int steps_per_launch,
+                                  int switch_below);
 
 /* ------------------------------------------------------------------------
  * SIA integrators (libtupan_gb300.so only).  No counterpart in the

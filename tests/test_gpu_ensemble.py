@@ -1,5 +1,5 @@
-"""Ensemble driver (batched persistent SPLIT sweeps, per-system steps)
-against the fp64 integrator oracle run system by system."""
+"""Ensemble driver (batched persistent SPLIT sweeps, or one CTA per system,
+per-system steps) against the fp64 integrator oracle run system by system."""
 
 import numpy as np
 import pytest
@@ -9,11 +9,18 @@ from tupan_gb300.ensemble import DeviceEnsemble, make_systems
 
 pytestmark = pytest.mark.gpu
 
+# (mode, steps per persistent launch, switch to batched below this many
+# systems): batched only; persistent to the end in launches of 3 steps;
+# persistent launches of 5 steps handing the last systems to batched mode
+MODES = [("batched", 1024, 0), ("persistent", 3, 0), ("persistent", 5, 8)]
 
-def test_ensemble_matches_per_system_oracle():
+
+@pytest.mark.parametrize("mode", MODES)
+def test_ensemble_matches_per_system_oracle(mode):
     systems = make_systems(24, lo=3, hi=120, seed=5)
     t_end, eta = 1.0 / 32, 1.0 / 64
     ens = DeviceEnsemble(systems, eta)
+    ens.set_mode(*mode)
     ke0, pe0 = ens.energies()
     ens.evolve(t_end, batch=4)
     t, k, st = ens.state()
@@ -36,21 +43,54 @@ def test_ensemble_matches_per_system_oracle():
     ens.close()
 
 
-def test_ensemble_systems_of_every_size_finish():
+@pytest.mark.parametrize("mode", MODES)
+def test_ensemble_systems_of_every_size_finish(mode):
     systems = make_systems(300, lo=3, hi=512, seed=9)
     ens = DeviceEnsemble(systems, 1.0 / 64)
+    ens.set_mode(*mode)
     ens.evolve(1.0 / 64, batch=8)
     t, k, _ = ens.state()
     assert np.all(t == 1.0 / 64) and np.all(k >= 1)
     ens.close()
 
 
-def test_ensemble_evolve_in_stages_reaches_each_end_time():
+@pytest.mark.parametrize("mode", MODES)
+def test_ensemble_evolve_in_stages_reaches_each_end_time(mode):
     # the captured step graph must pick up the t_end of each evolve call
     systems = make_systems(40, lo=3, hi=200, seed=10)
     ens = DeviceEnsemble(systems, 1.0 / 64)
+    ens.set_mode(*mode)
     for t_end in (1.0 / 256, 1.0 / 128, 1.0 / 64):
         ens.evolve(t_end, batch=4)
         t, k, _ = ens.state()
         assert np.all(t == t_end), (t_end, t.min(), t.max())
+    ens.close()
+
+
+def test_ensemble_persistent_matches_batched():
+    # the same stages and arithmetic; only the order of the j sums differs
+    # (FP32 sums agree to about 1e-7 of |a|, which a few steps carry into
+    # the state at a few 1e-9 of its scale)
+    systems = make_systems(60, lo=3, hi=512, seed=12)
+    out = []
+    for mode in (("batched", 1024, 0), ("persistent", 7, 0)):
+        ens = DeviceEnsemble(systems, 1.0 / 64)
+        ens.set_mode(*mode)
+        ens.evolve(1.0 / 128, batch=4)
+        out.append(ens.state())
+        ens.close()
+    (t0, k0, s0), (t1, k1, s1) = out
+    assert np.all(t0 == t1) and np.all(k0 == k1)
+    for c in ("rx", "ry", "rz", "vx", "vy", "vz"):
+        scale = np.abs(s0[c]).max()
+        assert np.max(np.abs(s0[c] - s1[c])) <= 1e-7 * scale, c
+
+
+def test_ensemble_set_mode_rejects_bad_arguments():
+    systems = make_systems(2, lo=3, hi=8, seed=1)
+    ens = DeviceEnsemble(systems, 1.0 / 64)
+    import tupan_gb300.lib as lib
+    for bad in (("persistent", 0, 0), ("persistent", 4, -1)):
+        with pytest.raises(lib.TupanGB300Error):
+            ens.set_mode(*bad)
     ens.close()

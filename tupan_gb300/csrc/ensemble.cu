@@ -160,18 +160,23 @@ k_e_begin(SysCtl *c, int *active, const unsigned *order, const uint64_t *off,
 
 // Packed record of particle i (the layout of split.cu's pack_records for 3
 // float4: {xh yh zh m} {xl yl zl e2} {vx vy vz 0}), from the current state.
-__device__ __forceinline__ void e_pack_one(const EArrays &A, float4 *out,
+__device__ __forceinline__ void e_pack_rec(const EArrays &A, float4 *r,
                                            uint64_t i)
 {
     float xh, xl, yh, yl, zh, zl;
     split2(A.r[0][i], xh, xl);
     split2(A.r[1][i], yh, yl);
     split2(A.r[2][i], zh, zl);
-    float4 *r = out + i * 3;
     r[0] = make_float4(xh, yh, zh, (float)A.m[i]);
     r[1] = make_float4(xl, yl, zl, (float)A.e2[i]);
     r[2] = make_float4((float)A.v[0][i], (float)A.v[1][i], (float)A.v[2][i],
                        0.f);
+}
+
+__device__ __forceinline__ void e_pack_one(const EArrays &A, float4 *out,
+                                           uint64_t i)
+{
+    e_pack_rec(A, out + i * 3, i);
 }
 
 // Records of every particle (before the first step of an evolve call).
@@ -227,35 +232,49 @@ __device__ void epi_step_size(const EArrays &A, SysCtl *c, uint64_t s,
     __syncthreads();
 }
 
-// H4.epredict (hermite.py:83-88), then the records of the predicted state.
+// H4.epredict (hermite.py:83-88) of particle i.
+__device__ __forceinline__ void predict_one(const EArrays &A, double tau,
+                                            uint64_t i)
+{
+    for (int d = 0; d < 3; ++d) {
+        const double a = A.f0[d][i], j = A.f0[3 + d][i], v = A.v[d][i];
+        A.r[d][i] = A.r[d][i] + ((j * tau / 3 + a) * tau / 2 + v) * tau;
+        A.v[d][i] = v + (j * tau / 2 + a) * tau;
+    }
+}
+
+// H4.ecorrect (hermite.py:96-119) of particle i.
+__device__ __forceinline__ void correct_one(const EArrays &A, double tau,
+                                            uint64_t i)
+{
+    for (int d = 0; d < 3; ++d) {
+        const double a0 = A.f0[d][i], a1 = A.f1[d][i];
+        const double j0 = A.f0[3 + d][i], j1 = A.f1[3 + d][i];
+        const double v0 = A.v0[d][i], r0 = A.r0[d][i];
+        const double v1 = (((j0 - j1) * tau / 6 + (a0 + a1)) * tau / 2 + v0);
+        A.v[d][i] = v1;
+        A.r[d][i] = (((a0 - a1) * tau / 6 + (v0 + v1)) * tau / 2 + r0);
+    }
+}
+
+// the predictor on an i-block, then the records of the predicted state
 __device__ void epi_predict(const EArrays &A, const SysCtl *c, float4 *rec,
                             uint64_t s, uint64_t b, uint64_t e)
 {
     const double tau = c[s].tau;
     for (uint64_t i = b + threadIdx.x; i < e; i += blockDim.x) {
-        for (int d = 0; d < 3; ++d) {
-            const double a = A.f0[d][i], j = A.f0[3 + d][i], v = A.v[d][i];
-            A.r[d][i] = A.r[d][i] + ((j * tau / 3 + a) * tau / 2 + v) * tau;
-            A.v[d][i] = v + (j * tau / 2 + a) * tau;
-        }
+        predict_one(A, tau, i);
         e_pack_one(A, rec, i);
     }
 }
 
-// H4.ecorrect (hermite.py:96-119), then the records of the corrected state.
+// the corrector on an i-block, then the records of the corrected state
 __device__ void epi_correct(const EArrays &A, const SysCtl *c, float4 *rec,
                             uint64_t s, uint64_t b, uint64_t e)
 {
     const double tau = c[s].tau;
     for (uint64_t i = b + threadIdx.x; i < e; i += blockDim.x) {
-        for (int d = 0; d < 3; ++d) {
-            const double a0 = A.f0[d][i], a1 = A.f1[d][i];
-            const double j0 = A.f0[3 + d][i], j1 = A.f1[3 + d][i];
-            const double v0 = A.v0[d][i], r0 = A.r0[d][i];
-            const double v1 = (((j0 - j1) * tau / 6 + (a0 + a1)) * tau / 2 + v0);
-            A.v[d][i] = v1;
-            A.r[d][i] = (((a0 - a1) * tau / 6 + (v0 + v1)) * tau / 2 + r0);
-        }
+        correct_one(A, tau, i);
         e_pack_one(A, rec, i);
     }
 }
@@ -290,11 +309,12 @@ struct BatchLaunch {
     float4 *rec_out;          // records written by the epilogues
 };
 
-// One system's i-range [ib, ib + ni) against all of its j.
+// One system's i-range [ib, ib + ni) against all of its j (records in
+// shared memory); outputs to out[c][b + i].
 template <class Op, bool X2>
-__device__ __forceinline__ void batched_block(const BatchLaunch &L,
-                                              const float4 *rec, uint64_t b,
-                                              int n, int ib, int ni)
+__device__ __forceinline__ void batched_block(double *const *out, float eta,
+                                              double eta_d, const float4 *rec,
+                                              uint64_t b, int n, int ib, int ni)
 {
     constexpr int NF = Op::NF, NO = Op::NO, MAXC = Op::MAXC;
     constexpr int NI = X2 ? 2 : 1;               // i per thread
@@ -337,7 +357,7 @@ __device__ __forceinline__ void batched_block(const BatchLaunch &L,
                 for (int c = 0; c < NO; ++c) p2[c] = make_float2(0.f, 0.f);
                 const int je = j0 + 16 * lanes < n ? j0 + 16 * lanes : n;
                 for (int j = j0; j < je; j += lanes)
-                    OpX2::pair(ip2, Op::load(rec + j * NF), p2, L.eta);
+                    OpX2::pair(ip2, Op::load(rec + j * NF), p2, eta);
 #pragma unroll
                 for (int c = 0; c < NO; ++c) {
                     part[0][c] = p2[c].x;
@@ -350,7 +370,7 @@ __device__ __forceinline__ void batched_block(const BatchLaunch &L,
             for (int j0 = lane; j0 < n; j0 += 16 * lanes) {
                 const int je = j0 + 16 * lanes < n ? j0 + 16 * lanes : n;
                 for (int j = j0; j < je; j += lanes)
-                    Op::pair(ip, Op::load(rec + j * NF), part[0], L.eta);
+                    Op::pair(ip, Op::load(rec + j * NF), part[0], eta);
                 fold();
             }
         }
@@ -368,9 +388,9 @@ __device__ __forceinline__ void batched_block(const BatchLaunch &L,
             }
             const int q = u0 * NI + k;
             if (lane == 0 && u0 < units && q < ni) {
-                Op::finish(v, L.eta_d);
+                Op::finish(v, eta_d);
 #pragma unroll
-                for (int c = 0; c < NO; ++c) L.out[c][b + iv[k]] = v[c];
+                for (int c = 0; c < NO; ++c) out[c][b + iv[k]] = v[c];
             }
         }
     }
@@ -416,7 +436,7 @@ k_e_sweep(const BatchLaunch L)
         bool got = mbar_wait_bounded(&bar, phase, L.err);
         phase ^= 1u;
         if (!__syncthreads_and(got)) break;
-        batched_block<Op, X2>(L, rec, b, n, ib, ie - ib);
+        batched_block<Op, X2>(L.out, L.eta, L.eta_d, rec, b, n, ib, ie - ib);
         __syncthreads();   // this block's forces are written (CTA scope)
         const uint64_t bi = b + ib, ei = b + ie;
         if (L.epi == EPI_STEP_SIZE) {
@@ -444,6 +464,107 @@ k_e_sweep(const BatchLaunch L)
             }
         }
         __syncthreads();   // the records of this system are no longer read
+    }
+}
+
+// ---------------------------------------------------------------------------
+// Persistent mode: each CTA takes a whole system from a queue (largest
+// first) and steps it on its own, with the system's packed records resident
+// in shared memory and __syncthreads between the stages, for up to
+// `max_steps` steps or until t_end; then it takes the next system.  No CTA
+// waits on another.  The stages and their arithmetic are those of the
+// batched mode (Tstep -> step size, AccJerk -> predict, AccJerk -> correct,
+// AccJerk -> correct); only the order of the j sums differs.
+// ---------------------------------------------------------------------------
+struct RunLaunch {
+    EArrays A;
+    SysCtl *ctl;
+    const uint64_t *off;
+    const unsigned *order;
+    unsigned ns;
+    unsigned *queue;
+    const double *t_end_p;
+    double eta;
+    int max_steps;
+    unsigned *err;
+};
+
+__global__ void __launch_bounds__(BATCH_NT, 2)
+k_e_run(const RunLaunch R)
+{
+    __shared__ __align__(16) float4 rec[BATCH_MAXN * 3];
+    __shared__ double red[BATCH_NT / 32];
+    __shared__ unsigned item;
+    const int tid = threadIdx.x;
+    const double t_end = *R.t_end_p;
+    const EArrays &A = R.A;
+    for (;;) {
+        if (tid == 0) item = atomicAdd(R.queue, 1u);
+        __syncthreads();
+        const unsigned w = item;
+        __syncthreads();               // `item` is rewritten next round
+        if (w >= R.ns) break;
+        const unsigned s = R.order[w];
+        const uint64_t b = R.off[s];
+        const int n = (int)(R.off[s + 1] - b);
+        if (n > BATCH_MAXN) {
+            if (tid == 0) atomicOr(R.err, (unsigned)DERR_BAD_LAUNCH);
+            continue;
+        }
+        double t = R.ctl[s].t;
+        long long steps = R.ctl[s].nsteps;
+        if (n < 1 || !(fabs(t) < t_end)) continue;
+        for (int i = tid; i < n; i += BATCH_NT) e_pack_rec(A, rec + 3 * i, b + i);
+        __syncthreads();
+        for (int k = 0; k < R.max_steps && fabs(t) < t_end; ++k) {
+            // step size: Tstep sweep, min |dt_a| over the system, quantised
+            const double tau0 = e_base_tstep(t, t_end, R.eta);
+            batched_block<TstepS, true>(A.dt, (float)R.eta, R.eta, rec, b, n,
+                                        0, n);
+            __syncthreads();
+            double m = INFINITY;
+            for (int i = tid; i < n; i += BATCH_NT)
+                m = fmin(m, fabs(A.dt[0][b + i]));
+            for (int o = 16; o > 0; o >>= 1)
+                m = fmin(m, __shfl_xor_sync(0xffffffffu, m, o));
+            if ((tid & 31) == 0) red[tid >> 5] = m;
+            __syncthreads();
+            if (tid == 0) {
+                for (int q = 1; q < BATCH_NT / 32; ++q) m = fmin(m, red[q]);
+                red[0] = e_block_tstep(m, t, tau0);
+            }
+            __syncthreads();
+            const double tau = red[0];
+            for (int i = tid; i < n; i += BATCH_NT)
+                for (int d = 0; d < 3; ++d) {
+                    A.r0[d][b + i] = A.r[d][b + i];
+                    A.v0[d][b + i] = A.v[d][b + i];
+                }
+            // P(EC)^2: forces at the start, predict, two corrections
+            batched_block<AccJerkS, true>(A.f0, 0.f, 0.0, rec, b, n, 0, n);
+            __syncthreads();
+            for (int i = tid; i < n; i += BATCH_NT) {
+                predict_one(A, tau, b + i);
+                e_pack_rec(A, rec + 3 * i, b + i);
+            }
+            __syncthreads();
+            for (int pass = 0; pass < 2; ++pass) {
+                batched_block<AccJerkS, true>(A.f1, 0.f, 0.0, rec, b, n, 0, n);
+                __syncthreads();
+                for (int i = tid; i < n; i += BATCH_NT) {
+                    correct_one(A, tau, b + i);
+                    e_pack_rec(A, rec + 3 * i, b + i);
+                }
+                __syncthreads();
+            }
+            t += tau;
+            steps += 1;
+        }
+        if (tid == 0) {
+            R.ctl[s].t = t;
+            R.ctl[s].nsteps = steps;
+        }
+        __syncthreads();
     }
 }
 
@@ -515,6 +636,9 @@ struct Ensemble {
     cudaGraphExec_t graph = nullptr;
     int graph_batch = -1;
     unsigned long long launches_per_batch = 0;
+    int mode = 0;                   // 0 batched steps, 1 persistent systems
+    int steps_per_launch = 1024;    // persistent: cap per system and launch
+    unsigned switch_below = 0;      // persistent -> batched below this many
 };
 
 unsigned grid_for(uint64_t n, int sms)
@@ -686,8 +810,53 @@ TG_EXPORT int tupan_gb300_ensemble_create(unsigned n_sys,
     return ST_OK;
 }
 
-// Steps every system until it reaches t_end (a graph of `batch` steps per
-// host check).  Returns the largest step count over the systems.
+// Persistent launches until every system reaches t_end or fewer than
+// E->switch_below systems are left.
+static int evolve_persistent(Ensemble *E, double t_end)
+{
+    std::vector<SysCtl> c(E->ns);
+    long long last_steps = -1;
+    for (;;) {
+        if (cudaMemcpy(c.data(), E->ctl, E->ns * sizeof(SysCtl),
+                       cudaMemcpyDeviceToHost) != cudaSuccess)
+            return ST_CUDA;
+        unsigned left = 0;
+        long long steps = 0;
+        for (unsigned s = 0; s < E->ns; ++s) {
+            if (fabs(c[s].t) < t_end) ++left;
+            steps += c[s].nsteps;
+        }
+        if (left == 0 || left < E->switch_below) return ST_OK;
+        if (steps == last_steps) return ST_DEVICE;
+        last_steps = steps;
+        RunLaunch R;
+        R.A = E->A;
+        R.ctl = E->ctl;
+        R.off = E->off;
+        R.order = E->order;
+        R.ns = E->ns;
+        R.queue = E->queue;
+        R.t_end_p = E->d_tend;
+        R.eta = E->eta;
+        R.max_steps = E->steps_per_launch;
+        R.err = E->err;
+        const unsigned grid = (unsigned)std::min<uint64_t>(
+            (uint64_t)E->sms * 2, (uint64_t)left);
+        if (cudaMemsetAsync(E->queue, 0, sizeof(unsigned), E->stream) !=
+            cudaSuccess)
+            return ST_CUDA;
+        k_e_run<<<grid, BATCH_NT, 0, E->stream>>>(R);
+        g_launch_count += 1;
+        if (cudaGetLastError() != cudaSuccess ||
+            cudaStreamSynchronize(E->stream) != cudaSuccess)
+            return ST_CUDA;
+    }
+}
+
+// Steps every system until it reaches t_end: persistent launches (mode 1)
+// while at least `switch_below` systems are left, then batched steps (a
+// graph of `batch` steps per host check).  Returns the largest step count
+// over the systems.
 TG_EXPORT int tupan_gb300_ensemble_evolve(void *handle, double t_end, int batch,
                                           long long *max_steps_out)
 {
@@ -698,6 +867,10 @@ TG_EXPORT int tupan_gb300_ensemble_evolve(void *handle, double t_end, int batch,
     if (cudaMemcpy(E->d_tend, &t_end, sizeof(double), cudaMemcpyHostToDevice) !=
         cudaSuccess)
         return ST_CUDA;
+    if (E->mode == 1) {
+        const int rc = evolve_persistent(E, t_end);
+        if (rc != ST_OK) return rc;
+    }
     // records of the current state for the first step's sweeps
     k_e_pack_all<<<(unsigned)E->sms * 8, 256, 0, E->stream>>>(E->A, E->n,
                                                                E->pack);
@@ -752,6 +925,22 @@ TG_EXPORT int tupan_gb300_ensemble_evolve(void *handle, double t_end, int batch,
     unsigned h = 0;
     cudaMemcpy(&h, E->err, sizeof(unsigned), cudaMemcpyDeviceToHost);
     return h ? ST_DEVICE : ST_OK;
+}
+
+// mode 0: every step of every system in batched launches; mode 1: one CTA
+// per system for up to steps_per_launch steps per launch, the last
+// switch_below - 1 systems in batched mode (0: persistent to the end).
+TG_EXPORT int tupan_gb300_ensemble_set_mode(void *handle, int mode,
+                                            int steps_per_launch,
+                                            int switch_below)
+{
+    Ensemble *E = (Ensemble *)handle;
+    if (!E || mode < 0 || mode > 1 || steps_per_launch < 1 || switch_below < 0)
+        return ST_BAD_ARGUMENT;
+    E->mode = mode;
+    E->steps_per_launch = steps_per_launch;
+    E->switch_below = (unsigned)switch_below;
+    return ST_OK;
 }
 
 // fp64 kinetic and potential energy of every system (HOST arrays of n_sys).

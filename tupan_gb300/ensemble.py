@@ -1,6 +1,7 @@
 """Ensembles of independent N-body systems on one GPU (csrc/ensemble.cu):
-each system has its own shared adaptive Hermite-4 step; every force
-evaluation of the ensemble is one persistent batched SPLIT launch."""
+each system has its own shared adaptive Hermite-4 step.  Batched mode: every
+force evaluation of the ensemble is one persistent batched SPLIT launch;
+persistent mode: one CTA steps one whole system at a time."""
 
 import ctypes
 
@@ -28,6 +29,9 @@ def _declare(L):
     L.tupan_gb300_ensemble_get.restype = c.c_int
     L.tupan_gb300_ensemble_destroy.argtypes = [c.c_void_p]
     L.tupan_gb300_ensemble_destroy.restype = c.c_int
+    L.tupan_gb300_ensemble_set_mode.argtypes = [c.c_void_p, c.c_int, c.c_int,
+                                                c.c_int]
+    L.tupan_gb300_ensemble_set_mode.restype = c.c_int
 
 
 def make_systems(count, lo=3, hi=512, eps=1e-4, seed=1):
@@ -57,6 +61,18 @@ class DeviceEnsemble(object):
         self.h = h
         self.n_sys = len(systems)
         self.n = int(self.off[-1])
+
+    def set_mode(self, mode, steps_per_launch=1024, switch_below=0):
+        """"batched": every step of all systems as five launches (graph of
+        `batch` steps); "persistent": one CTA per system for up to
+        steps_per_launch steps per launch, handing the last systems (fewer
+        than switch_below) to the batched mode."""
+        m = {"batched": 0, "persistent": 1}[mode]
+        st = self.L.tupan_gb300_ensemble_set_mode(
+            self.h, m, int(steps_per_launch), int(switch_below))
+        if st:
+            raise lib.TupanGB300Error("ensemble_set_mode failed: status %d"
+                                      % st)
 
     def evolve(self, t_end, batch=8):
         mx = ctypes.c_longlong()

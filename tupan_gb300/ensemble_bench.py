@@ -22,11 +22,16 @@ def main(argv=None):
     ap.add_argument("--t-end", type=float, default=1.0 / 16)
     ap.add_argument("--eta", type=float, default=1.0 / 64)
     ap.add_argument("--batch", type=int, default=16)
+    ap.add_argument("--mode", default="batched",
+                    choices=["batched", "persistent"])
+    ap.add_argument("--steps-per-launch", type=int, default=1024)
+    ap.add_argument("--switch-below", type=int, default=0)
     a = ap.parse_args(argv)
     from .ensemble import DeviceEnsemble, make_systems
     t0 = time.perf_counter()
     systems = make_systems(a.systems, seed=1)
     ens = DeviceEnsemble(systems, a.eta)
+    ens.set_mode(a.mode, a.steps_per_launch, a.switch_below)
     ke0, pe0 = ens.energies()
     t1 = time.perf_counter()
     mx = ens.evolve(a.t_end, batch=a.batch)
@@ -37,6 +42,8 @@ def main(argv=None):
     de = np.abs(((ke1 + pe1) - (ke0 + pe0)) / -pe0)
     print(json.dumps({
         "systems": a.systems, "particles": int(ens.n), "t_end": a.t_end,
+        "mode": a.mode, "steps_per_launch": a.steps_per_launch,
+        "switch_below": a.switch_below,
         "wall_s": t2 - t1, "setup_s": t1 - t0,
         "systems_per_s": a.systems / (t2 - t1),
         "max_steps": int(mx), "mean_steps": float(k.mean()),
