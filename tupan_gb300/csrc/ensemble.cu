@@ -288,6 +288,9 @@ __device__ void epi_correct(const EArrays &A, const SysCtl *c, float4 *rec,
 // The CTA that completes the last item of a system runs the step's next
 // per-system stage (the epilogue), so a Hermite step is five launches.
 // ---------------------------------------------------------------------------
+// AccJerk with 1/sqrt from rsqrtf alone (the split sweeps' default form)
+using AccJerkFast = AccJerkSN<false>;
+
 constexpr int BATCH_NT = 256;
 constexpr int BATCH_MAXN = 512;           // largest system held in smem
 
@@ -541,7 +544,7 @@ k_e_run(const RunLaunch R)
                     A.v0[d][b + i] = A.v[d][b + i];
                 }
             // P(EC)^2: forces at the start, predict, two corrections
-            batched_block<AccJerkS, true>(A.f0, 0.f, 0.0, rec, b, n, 0, n);
+            batched_block<AccJerkFast, true>(A.f0, 0.f, 0.0, rec, b, n, 0, n);
             __syncthreads();
             for (int i = tid; i < n; i += BATCH_NT) {
                 predict_one(A, tau, b + i);
@@ -549,7 +552,7 @@ k_e_run(const RunLaunch R)
             }
             __syncthreads();
             for (int pass = 0; pass < 2; ++pass) {
-                batched_block<AccJerkS, true>(A.f1, 0.f, 0.0, rec, b, n, 0, n);
+                batched_block<AccJerkFast, true>(A.f1, 0.f, 0.0, rec, b, n, 0, n);
                 __syncthreads();
                 for (int i = tid; i < n; i += BATCH_NT) {
                     correct_one(A, tau, b + i);
@@ -677,7 +680,7 @@ cudaError_t e_sweep(Ensemble *E, int kernel, double *const *out, double eta,
     if (kernel == K_TSTEP)
         k_e_sweep<TstepS><<<grid, BATCH_NT, 0, E->stream>>>(L);
     else
-        k_e_sweep<AccJerkS><<<grid, BATCH_NT, 0, E->stream>>>(L);
+        k_e_sweep<AccJerkFast><<<grid, BATCH_NT, 0, E->stream>>>(L);
     g_launch_count += 1;
     return cudaGetLastError();
 }

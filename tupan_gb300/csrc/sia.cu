@@ -395,7 +395,7 @@ __device__ void sub_split_sweep(SubState &S, int ilo, int ni, int jlo, int nj,
 __device__ void sub_acc(SubState &S, int ilo, int ni, int jlo, int nj,
                         const SubParams &P, const Sweep &acc)
 {
-    if (P.split) sub_split_sweep<AccS>(S, ilo, ni, jlo, nj, F_AX, 0.0);
+    if (P.split) sub_split_sweep<AccSN<false>>(S, ilo, ni, jlo, nj, F_AX, 0.0);
     else sub_sweep<AccPair<double>>(S, ilo, ni, jlo, nj, F_AX, acc);
 }
 
