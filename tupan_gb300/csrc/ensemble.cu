@@ -358,9 +358,16 @@ __device__ __forceinline__ void batched_block(double *const *out, float eta,
                 float2 p2[NO];
 #pragma unroll
                 for (int c = 0; c < NO; ++c) p2[c] = make_float2(0.f, 0.f);
-                const int je = j0 + 16 * lanes < n ? j0 + 16 * lanes : n;
-                for (int j = j0; j < je; j += lanes)
-                    OpX2::pair(ip2, Op::load(rec + j * NF), p2, eta);
+                if (j0 + 15 * lanes < n) {
+                    // a whole run: unrolled, so independent pairs interleave
+#pragma unroll
+                    for (int u = 0; u < 16; ++u)
+                        OpX2::pair(ip2, Op::load(rec + (j0 + u * lanes) * NF),
+                                   p2, eta);
+                } else {
+                    for (int j = j0; j < n; j += lanes)
+                        OpX2::pair(ip2, Op::load(rec + j * NF), p2, eta);
+                }
 #pragma unroll
                 for (int c = 0; c < NO; ++c) {
                     part[0][c] = p2[c].x;
@@ -371,9 +378,15 @@ __device__ __forceinline__ void batched_block(double *const *out, float eta,
         } else {
             const typename Op::P ip = Op::load(rec + iv[0] * NF);
             for (int j0 = lane; j0 < n; j0 += 16 * lanes) {
-                const int je = j0 + 16 * lanes < n ? j0 + 16 * lanes : n;
-                for (int j = j0; j < je; j += lanes)
-                    Op::pair(ip, Op::load(rec + j * NF), part[0], eta);
+                if (j0 + 15 * lanes < n) {
+#pragma unroll
+                    for (int u = 0; u < 16; ++u)
+                        Op::pair(ip, Op::load(rec + (j0 + u * lanes) * NF),
+                                 part[0], eta);
+                } else {
+                    for (int j = j0; j < n; j += lanes)
+                        Op::pair(ip, Op::load(rec + j * NF), part[0], eta);
+                }
                 fold();
             }
         }
