@@ -288,8 +288,10 @@ __device__ void epi_correct(const EArrays &A, const SysCtl *c, float4 *rec,
 // The CTA that completes the last item of a system runs the step's next
 // per-system stage (the epilogue), so a Hermite step is five launches.
 // ---------------------------------------------------------------------------
-// AccJerk with 1/sqrt from rsqrtf alone (the split sweeps' default form)
+// AccJerk and Tstep with 1/sqrt from rsqrtf alone (the split sweeps'
+// default forms)
 using AccJerkFast = AccJerkSN<false>;
+using TstepFast = TstepSN<false>;
 
 constexpr int BATCH_NT = 256;
 constexpr int BATCH_MAXN = 512;           // largest system held in smem
@@ -535,7 +537,7 @@ k_e_run(const RunLaunch R)
         for (int k = 0; k < R.max_steps && fabs(t) < t_end; ++k) {
             // step size: Tstep sweep, min |dt_a| over the system, quantised
             const double tau0 = e_base_tstep(t, t_end, R.eta);
-            batched_block<TstepS, true>(A.dt, (float)R.eta, R.eta, rec, b, n,
+            batched_block<TstepFast, true>(A.dt, (float)R.eta, R.eta, rec, b, n,
                                         0, n);
             __syncthreads();
             double m = INFINITY;
@@ -691,7 +693,7 @@ cudaError_t e_sweep(Ensemble *E, int kernel, double *const *out, double eta,
     const unsigned grid = (unsigned)((uint64_t)E->sms * 2 < max_items
                                          ? (uint64_t)E->sms * 2 : max_items);
     if (kernel == K_TSTEP)
-        k_e_sweep<TstepS><<<grid, BATCH_NT, 0, E->stream>>>(L);
+        k_e_sweep<TstepFast><<<grid, BATCH_NT, 0, E->stream>>>(L);
     else
         k_e_sweep<AccJerkFast><<<grid, BATCH_NT, 0, E->stream>>>(L);
     g_launch_count += 1;

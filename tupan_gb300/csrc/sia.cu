@@ -490,7 +490,7 @@ __device__ void sub_enter(SubState &S, int lo, int n, double tau,
     if (P.mode != 's') {
         flag = 1.0;
         if (P.split)
-            sub_split_sweep<TstepS>(S, lo, n, lo, n, F_TSTEP, P.eta);
+            sub_split_sweep<TstepSN<false>>(S, lo, n, lo, n, F_TSTEP, P.eta);
         else
             sub_sweep<TstepPair<double>>(S, lo, n, lo, n, F_TSTEP, tst);
         if (P.mode == 'a') {

@@ -130,7 +130,8 @@ struct AccJerkSN {
 using AccJerkS = AccJerkSN<true>;
 
 // tstep_kernel_common.h:7-60 in FP32; output 0 sums w2, output 1 is max w2.
-struct TstepS {
+template <bool NR>
+struct TstepSN {
     static constexpr int NF = 3, NO = 2, MAXC = 1;
     using P = AccJerkS::P;
     __device__ static P load(const float4 *r) { return AccJerkS::load(r); }
@@ -145,12 +146,12 @@ struct TstepS {
         float s = fmaf(dz, dz, fmaf(dy, dy, fmaf(dx, dx, h2)));
         float rv = fmaf(dz, uz, fmaf(dy, uy, dx * ux));
         float v2 = fmaf(uz, uz, fmaf(uy, uy, ux * ux));
-        float y = rsqrt_nr(s);
+        float y = rsq<NR>(s);
         float q = y * y;
         float phi = msum * y;
         float w2 = q * fmaf(2.0f, phi, v2);
         float g = q * fmaf(2.0f * q, phi, w2);
-        g *= eta * rsqrt_nr(w2);
+        g *= eta * rsq<NR>(w2);
         w2 = fmaf(-g, rv, w2);
         w2 = (s > h2) ? w2 : 0.0f;
         acc[0] += w2;
@@ -162,6 +163,7 @@ struct TstepS {
         v[1] = eta / sqrt(1.0 + v[1]);
     }
 };
+using TstepS = TstepSN<true>;
 
 // snap_crackle_kernel_common.h:7-95 in FP32 (all differences j - i).
 struct SnapS {
@@ -389,7 +391,15 @@ __device__ __forceinline__ float2 rsqrt_nr2_raw(float2 s)
     return mul2(y, fma2(u, dup(-0.5f), dup(1.5f)));
 }
 
-struct TstepS2 {
+template <bool NR>
+__device__ __forceinline__ float2 rsq2_unmasked(float2 s)
+{
+    if constexpr (NR) return rsqrt_nr2_raw(s);
+    return make_float2(rsqrtf(s.x), rsqrtf(s.y));
+}
+
+template <bool NR>
+struct TstepS2N {
     static constexpr bool HAS_H2 = false;
     using P = AccJerkS::P;
     using I = PosVelMI2;
@@ -415,12 +425,12 @@ struct TstepS2 {
         float2 s = fma2(dz, dz, fma2(dy, dy, fma2(dx, dx, h2)));
         float2 rv = fma2(dz, uz, fma2(dy, uy, mul2(dx, ux)));
         float2 v2 = fma2(uz, uz, fma2(uy, uy, mul2(ux, ux)));
-        float2 y = rsqrt_nr2_raw(s);
+        float2 y = rsq2_unmasked<NR>(s);
         float2 q = mul2(y, y);
         float2 phi = mul2(msum, y);
         float2 w2 = mul2(q, fma2(dup(2.0f), phi, v2));
         float2 g = mul2(q, fma2(mul2(dup(2.0f), q), phi, w2));
-        g = mul2(g, mul2(dup(eta), rsqrt_nr2_raw(w2)));
+        g = mul2(g, mul2(dup(eta), rsq2_unmasked<NR>(w2)));
         w2 = fma2(make_float2(-g.x, -g.y), rv, w2);
         w2.x = (s.x > h2.x) ? w2.x : 0.0f;
         w2.y = (s.y > h2.y) ? w2.y : 0.0f;
@@ -514,7 +524,7 @@ template <class Op> struct X2Of { using type = void; };
 template <bool NR> struct X2Of<PhiSN<NR>> { using type = PhiS2N<NR>; };
 template <bool NR> struct X2Of<AccSN<NR>> { using type = AccS2N<NR>; };
 template <bool NR> struct X2Of<AccJerkSN<NR>> { using type = AccJerkS2N<NR>; };
-template <> struct X2Of<TstepS> { using type = TstepS2; };
+template <bool NR> struct X2Of<TstepSN<NR>> { using type = TstepS2N<NR>; };
 template <> struct X2Of<SnapS> { using type = SnapS2; };
 
 }  // namespace tg
