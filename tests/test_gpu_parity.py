@@ -293,11 +293,9 @@ def test_split_no_newton_variants(name, variant):
 
 def test_split_model_prefers_no_newton_forms():
     for name in ("phi_kernel", "acc_kernel", "acc_jerk_kernel",
-                 "tstep_kernel"):
+                 "tstep_kernel", "snap_crackle_kernel"):
         v, g = lib.split_choice(name, 262144, 262144)
         assert v in (9, 11), (name, v, g)
-    v, g = lib.split_choice("snap_crackle_kernel", 262144, 262144)
-    assert v not in (9, 10, 11), v
 
 
 @pytest.mark.parametrize("variant", range(12))

@@ -392,19 +392,19 @@ void split_variant_info(int v, int *ni_per_thread, int *jsplit, int *threads)
     *threads = kVariants[v].threads;
 }
 
-// Variants 9 to 11 take 1/sqrt from the MUFU approximation alone; the
-// operators with that form are Phi, Acc, AccJerk and Tstep (SnapCrackle
-// runs its Newton-step form under those numbers).
+// Variants 9 to 11 take 1/sqrt from the MUFU approximation alone (every
+// SPLIT operator has that form).
 template <class Op> struct RawOf { using type = Op; };
 template <> struct RawOf<PhiS> { using type = PhiSN<false>; };
 template <> struct RawOf<AccS> { using type = AccSN<false>; };
 template <> struct RawOf<AccJerkS> { using type = AccJerkSN<false>; };
 template <> struct RawOf<TstepS> { using type = TstepSN<false>; };
+template <> struct RawOf<SnapS> { using type = SnapSN<false>; };
 
 bool split_has_raw(int kernel)
 {
     return kernel == K_PHI || kernel == K_ACC || kernel == K_ACC_JERK ||
-           kernel == K_TSTEP;
+           kernel == K_TSTEP || kernel == K_SNAP_CRACKLE;
 }
 
 // Kernels with a packed-pair (f32x2) operator: variants 5 to 10 use it.

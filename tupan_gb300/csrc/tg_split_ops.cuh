@@ -166,12 +166,16 @@ struct TstepSN {
 using TstepS = TstepSN<true>;
 
 // snap_crackle_kernel_common.h:7-95 in FP32 (all differences j - i).
-struct SnapS {
+// Register image of a SnapCrackle record (position, velocity, a, j).
+struct SnapRec {
+    float xh, yh, zh, m, xl, yl, zl, e2, vx, vy, vz, ax, ay, az, jx, jy,
+        jz;
+};
+
+template <bool NR>
+struct SnapSN {
     static constexpr int NF = 5, NO = 6, MAXC = -1;
-    struct P {
-        float xh, yh, zh, m, xl, yl, zl, e2, vx, vy, vz, ax, ay, az, jx, jy,
-            jz;
-    };
+    using P = SnapRec;
     __device__ static P load(const float4 *r)
     {
         float4 a = r[0], b = r[1], c = r[2], d = r[3], e = r[4];
@@ -193,7 +197,7 @@ struct SnapS {
         float rJ = fmaf(dz, Jz, fmaf(dy, Jy, dx * Jx));
         float rA = fmaf(dz, Az, fmaf(dy, Ay, dx * Ax));
         float vA = fmaf(uz, Az, fmaf(uy, Ay, ux * Ax));
-        float y = rsqrt_nr(s);
+        float y = rsq<NR>(s);
         y = (s > h2) ? y : 0.0f;
         float q = y * y;
         float al = rv * q;
@@ -224,6 +228,7 @@ struct SnapS {
     }
     __device__ static void finish(double *, double) {}
 };
+using SnapS = SnapSN<true>;
 
 // Kahan-compensated FP32 accumulation of one run of pair terms.
 __device__ __forceinline__ void kahan_add(float &sum, float &corr, float x)
@@ -445,7 +450,8 @@ struct SnapI2 {
         njx, njy, njz;
 };
 
-struct SnapS2 {
+template <bool NR>
+struct SnapS2N {
     static constexpr bool HAS_H2 = false;
     using P = SnapS::P;
     using I = SnapI2;
@@ -481,7 +487,7 @@ struct SnapS2 {
         float2 rJ = fma2(dz, Jz, fma2(dy, Jy, mul2(dx, Jx)));
         float2 rA = fma2(dz, Az, fma2(dy, Ay, mul2(dx, Ax)));
         float2 vA = fma2(uz, Az, fma2(uy, Ay, mul2(ux, Ax)));
-        float2 y = rsqrt_nr2(s, h2);
+        float2 y = rsq2<NR>(s, h2);
         float2 q = mul2(y, y);
         float2 al = mul2(rv, q);
         float2 al2 = mul2(al, al);
@@ -525,6 +531,6 @@ template <bool NR> struct X2Of<PhiSN<NR>> { using type = PhiS2N<NR>; };
 template <bool NR> struct X2Of<AccSN<NR>> { using type = AccS2N<NR>; };
 template <bool NR> struct X2Of<AccJerkSN<NR>> { using type = AccJerkS2N<NR>; };
 template <bool NR> struct X2Of<TstepSN<NR>> { using type = TstepS2N<NR>; };
-template <> struct X2Of<SnapS> { using type = SnapS2; };
+template <bool NR> struct X2Of<SnapSN<NR>> { using type = SnapS2N<NR>; };
 
 }  // namespace tg
