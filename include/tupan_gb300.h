@@ -173,7 +173,9 @@ long long tupan_gb300_set_kepler_budget(long long budget);
 /* SPLIT-mode launch configuration: variant in [0, tupan_gb300_split_variants())
  * and grid j-split count; set_split_config forces it for a kernel
  * (variant < 0 restores the automatic choice), set_tuned records it for sizes
- * in the same power-of-two buckets, split_choice reports the choice. */
+ * in the same power-of-two buckets, split_choice reports the choice.
+ * Variants 0-8 form 1/sqrt as rsqrt plus one Newton step; 9, 10 and 11 are
+ * variants 5, 7 and 0 with rsqrt alone (the automatic choice). */
 int tupan_gb300_set_split_config(int kernel, int variant, int gsplit);
 int tupan_gb300_set_tuned(int kernel, uint64_t ni, uint64_t nj, int variant,
                           int gsplit);
