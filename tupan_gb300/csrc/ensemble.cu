@@ -293,7 +293,9 @@ __device__ void epi_correct(const EArrays &A, const SysCtl *c, float4 *rec,
 using AccJerkFast = AccJerkSN<false>;
 using TstepFast = TstepSN<false>;
 
-constexpr int BATCH_NT = 256;
+constexpr int BATCH_NT = 128;             // batched sweep: threads per CTA
+constexpr int BATCH_MINB = 4;             // and CTAs per SM
+constexpr int RUN_NT = 256;               // persistent mode: threads per CTA
 constexpr int BATCH_MAXN = 512;           // largest system held in smem
 
 struct BatchLaunch {
@@ -316,7 +318,7 @@ struct BatchLaunch {
 
 // One system's i-range [ib, ib + ni) against all of its j (records in
 // shared memory); outputs to out[c][b + i].
-template <class Op, bool X2>
+template <class Op, bool X2, int NT>
 __device__ __forceinline__ void batched_block(double *const *out, float eta,
                                               double eta_d, const float4 *rec,
                                               uint64_t b, int n, int ib, int ni)
@@ -326,8 +328,8 @@ __device__ __forceinline__ void batched_block(double *const *out, float eta,
     const int tid = threadIdx.x;
     const int units = (ni + NI - 1) / NI;        // i (pairs) of the block
     int lanes = 1;
-    while (lanes < 32 && lanes * 2 * units <= BATCH_NT) lanes *= 2;
-    const int groups = BATCH_NT / lanes;
+    while (lanes < 32 && lanes * 2 * units <= NT) lanes *= 2;
+    const int groups = NT / lanes;
     const int lane = tid % lanes;
     for (int u0 = tid / lanes; u0 - tid / lanes < units; u0 += groups) {
         const int u = u0 < units ? u0 : units - 1;
@@ -415,7 +417,7 @@ __device__ __forceinline__ void batched_block(double *const *out, float eta,
 }
 
 template <class Op>
-__global__ void __launch_bounds__(BATCH_NT, 2)
+__global__ void __launch_bounds__(BATCH_NT, BATCH_MINB)
 k_e_sweep(const BatchLaunch L)
 {
     constexpr int NF = Op::NF;
@@ -454,7 +456,8 @@ k_e_sweep(const BatchLaunch L)
         bool got = mbar_wait_bounded(&bar, phase, L.err);
         phase ^= 1u;
         if (!__syncthreads_and(got)) break;
-        batched_block<Op, X2>(L.out, L.eta, L.eta_d, rec, b, n, ib, ie - ib);
+        batched_block<Op, X2, BATCH_NT>(L.out, L.eta, L.eta_d, rec, b, n, ib,
+                                        ie - ib);
         __syncthreads();   // this block's forces are written (CTA scope)
         const uint64_t bi = b + ib, ei = b + ie;
         if (L.epi == EPI_STEP_SIZE) {
@@ -507,11 +510,11 @@ struct RunLaunch {
     unsigned *err;
 };
 
-__global__ void __launch_bounds__(BATCH_NT, 2)
+__global__ void __launch_bounds__(RUN_NT, 2)
 k_e_run(const RunLaunch R)
 {
     __shared__ __align__(16) float4 rec[BATCH_MAXN * 3];
-    __shared__ double red[BATCH_NT / 32];
+    __shared__ double red[RUN_NT / 32];
     __shared__ unsigned item;
     const int tid = threadIdx.x;
     const double t_end = *R.t_end_p;
@@ -532,44 +535,44 @@ k_e_run(const RunLaunch R)
         double t = R.ctl[s].t;
         long long steps = R.ctl[s].nsteps;
         if (n < 1 || !(fabs(t) < t_end)) continue;
-        for (int i = tid; i < n; i += BATCH_NT) e_pack_rec(A, rec + 3 * i, b + i);
+        for (int i = tid; i < n; i += RUN_NT) e_pack_rec(A, rec + 3 * i, b + i);
         __syncthreads();
         for (int k = 0; k < R.max_steps && fabs(t) < t_end; ++k) {
             // step size: Tstep sweep, min |dt_a| over the system, quantised
             const double tau0 = e_base_tstep(t, t_end, R.eta);
-            batched_block<TstepFast, true>(A.dt, (float)R.eta, R.eta, rec, b, n,
+            batched_block<TstepFast, true, RUN_NT>(A.dt, (float)R.eta, R.eta, rec, b, n,
                                         0, n);
             __syncthreads();
             double m = INFINITY;
-            for (int i = tid; i < n; i += BATCH_NT)
+            for (int i = tid; i < n; i += RUN_NT)
                 m = fmin(m, fabs(A.dt[0][b + i]));
             for (int o = 16; o > 0; o >>= 1)
                 m = fmin(m, __shfl_xor_sync(0xffffffffu, m, o));
             if ((tid & 31) == 0) red[tid >> 5] = m;
             __syncthreads();
             if (tid == 0) {
-                for (int q = 1; q < BATCH_NT / 32; ++q) m = fmin(m, red[q]);
+                for (int q = 1; q < RUN_NT / 32; ++q) m = fmin(m, red[q]);
                 red[0] = e_block_tstep(m, t, tau0);
             }
             __syncthreads();
             const double tau = red[0];
-            for (int i = tid; i < n; i += BATCH_NT)
+            for (int i = tid; i < n; i += RUN_NT)
                 for (int d = 0; d < 3; ++d) {
                     A.r0[d][b + i] = A.r[d][b + i];
                     A.v0[d][b + i] = A.v[d][b + i];
                 }
             // P(EC)^2: forces at the start, predict, two corrections
-            batched_block<AccJerkFast, true>(A.f0, 0.f, 0.0, rec, b, n, 0, n);
+            batched_block<AccJerkFast, true, RUN_NT>(A.f0, 0.f, 0.0, rec, b, n, 0, n);
             __syncthreads();
-            for (int i = tid; i < n; i += BATCH_NT) {
+            for (int i = tid; i < n; i += RUN_NT) {
                 predict_one(A, tau, b + i);
                 e_pack_rec(A, rec + 3 * i, b + i);
             }
             __syncthreads();
             for (int pass = 0; pass < 2; ++pass) {
-                batched_block<AccJerkFast, true>(A.f1, 0.f, 0.0, rec, b, n, 0, n);
+                batched_block<AccJerkFast, true, RUN_NT>(A.f1, 0.f, 0.0, rec, b, n, 0, n);
                 __syncthreads();
-                for (int i = tid; i < n; i += BATCH_NT) {
+                for (int i = tid; i < n; i += RUN_NT) {
                     correct_one(A, tau, b + i);
                     e_pack_rec(A, rec + 3 * i, b + i);
                 }
@@ -690,8 +693,8 @@ cudaError_t e_sweep(Ensemble *E, int kernel, double *const *out, double eta,
     L.rec_out = E->pack + (size_t)write_buf * E->n * 3;
     // persistent CTAs; a system of up to 512 particles is at most 16 items
     const uint64_t max_items = (uint64_t)E->ns * 16;
-    const unsigned grid = (unsigned)((uint64_t)E->sms * 2 < max_items
-                                         ? (uint64_t)E->sms * 2 : max_items);
+    const uint64_t ctas = (uint64_t)E->sms * BATCH_MINB;
+    const unsigned grid = (unsigned)(ctas < max_items ? ctas : max_items);
     if (kernel == K_TSTEP)
         k_e_sweep<TstepFast><<<grid, BATCH_NT, 0, E->stream>>>(L);
     else
@@ -711,7 +714,7 @@ cudaError_t e_step(Ensemble *E)
     cudaStream_t st = E->stream;
     k_e_begin<<<1, COMPACT_NT, 0, st>>>(E->ctl, E->active, E->order, E->off,
                                         E->ns, E->d_tend, E->eta,
-                                        (unsigned)E->sms * 2, E->alist,
+                                        (unsigned)E->sms * BATCH_MINB, E->alist,
                                         E->acount, E->items, E->icount,
                                         E->sys_items, E->queue);
     g_launch_count += 1;
@@ -863,7 +866,7 @@ static int evolve_persistent(Ensemble *E, double t_end)
         if (cudaMemsetAsync(E->queue, 0, sizeof(unsigned), E->stream) !=
             cudaSuccess)
             return ST_CUDA;
-        k_e_run<<<grid, BATCH_NT, 0, E->stream>>>(R);
+        k_e_run<<<grid, RUN_NT, 0, E->stream>>>(R);
         g_launch_count += 1;
         if (cudaGetLastError() != cudaSuccess ||
             cudaStreamSynchronize(E->stream) != cudaSuccess)
