@@ -257,28 +257,6 @@ __device__ __forceinline__ void correct_one(const EArrays &A, double tau,
     }
 }
 
-// the predictor on an i-block, then the records of the predicted state
-__device__ void epi_predict(const EArrays &A, const SysCtl *c, float4 *rec,
-                            uint64_t s, uint64_t b, uint64_t e)
-{
-    const double tau = c[s].tau;
-    for (uint64_t i = b + threadIdx.x; i < e; i += blockDim.x) {
-        predict_one(A, tau, i);
-        e_pack_one(A, rec, i);
-    }
-}
-
-// the corrector on an i-block, then the records of the corrected state
-__device__ void epi_correct(const EArrays &A, const SysCtl *c, float4 *rec,
-                            uint64_t s, uint64_t b, uint64_t e)
-{
-    const double tau = c[s].tau;
-    for (uint64_t i = b + threadIdx.x; i < e; i += blockDim.x) {
-        correct_one(A, tau, i);
-        e_pack_one(A, rec, i);
-    }
-}
-
 // ---------------------------------------------------------------------------
 // Batched SPLIT sweep over the (system, i-block) work items of the active
 // systems, one persistent launch per force evaluation.  CTAs take items
@@ -434,9 +412,9 @@ k_e_sweep(const BatchLaunch L)
     __syncthreads();
     const unsigned n_items = *L.n_items;
     uint32_t phase = 0;
+    if (tid == 0) item = atomicAdd(L.queue, 1u);
+    __syncthreads();
     for (;;) {
-        if (tid == 0) item = atomicAdd(L.queue, 1u);
-        __syncthreads();
         const unsigned w = item;
         if (w >= n_items) break;
         const unsigned sys = L.items[w].x;
@@ -456,35 +434,56 @@ k_e_sweep(const BatchLaunch L)
         bool got = mbar_wait_bounded(&bar, phase, L.err);
         phase ^= 1u;
         if (!__syncthreads_and(got)) break;
+        const uint64_t bi = b + ib, ei = b + ie;
+        // Tstep sweeps (the one operator with a max output) end in the
+        // step size; AccJerk sweeps in the predictor or corrector
+        constexpr bool TSTEP_SWEEP = Op::MAXC >= 0;
         batched_block<Op, X2, BATCH_NT>(L.out, L.eta, L.eta_d, rec, b, n, ib,
                                         ie - ib);
-        __syncthreads();   // this block's forces are written (CTA scope)
-        const uint64_t bi = b + ib, ei = b + ie;
-        if (L.epi == EPI_STEP_SIZE) {
-            epi_copy(L.A, bi, ei);
-            // publish this item's Tstep outputs, then count it; the CTA
-            // that completes the system takes the system's minimum
-            __threadfence();
-            __syncthreads();
-            if (tid == 0)
-                last = atomicAdd(&L.sys_done[sys], 1u) + 1u == L.sys_items[sys];
-            __syncthreads();
-            if (last) {
+        __syncthreads();   // this block's outputs are written (CTA scope)
+        if constexpr (TSTEP_SWEEP) {
+            if (L.epi == EPI_STEP_SIZE) {
+                epi_copy(L.A, bi, ei);
+                // publish this item's Tstep outputs, then count it; the
+                // CTA that completes the system takes the system's minimum
                 __threadfence();
-                epi_step_size(L.A, L.ctl, sys, b, b + n);
-                if (tid == 0) L.sys_done[sys] = 0;
+                __syncthreads();
+                if (tid == 0)
+                    last = atomicAdd(&L.sys_done[sys], 1u) + 1u ==
+                           L.sys_items[sys];
+                __syncthreads();
+                if (last) {
+                    __threadfence();
+                    epi_step_size(L.A, L.ctl, sys, b, b + n);
+                    if (tid == 0) L.sys_done[sys] = 0;
+                }
             }
-        } else if (L.epi == EPI_PREDICT) {
-            epi_predict(L.A, L.ctl, L.rec_out, sys, bi, ei);
-        } else if (L.epi == EPI_CORRECT || L.epi == EPI_CORRECT_END) {
-            epi_correct(L.A, L.ctl, L.rec_out, sys, bi, ei);
-            // the system's time moves once, by its first item
-            if (L.epi == EPI_CORRECT_END && ib == 0 && tid == 0) {
-                L.ctl[sys].t += L.ctl[sys].tau;
-                L.ctl[sys].nsteps += 1;
+        } else {
+            // the block's predictor or corrector, spread over the CTA;
+            // records go to the buffer the next sweep reads
+            const double tau = L.ctl[sys].tau;
+            if (L.epi == EPI_PREDICT) {
+                for (uint64_t i = bi + tid; i < ei; i += BATCH_NT) {
+                    predict_one(L.A, tau, i);
+                    e_pack_one(L.A, L.rec_out, i);
+                }
+            } else if (L.epi == EPI_CORRECT || L.epi == EPI_CORRECT_END) {
+                for (uint64_t i = bi + tid; i < ei; i += BATCH_NT) {
+                    correct_one(L.A, tau, i);
+                    e_pack_one(L.A, L.rec_out, i);
+                }
+                // the system's time moves once, by its first item
+                if (L.epi == EPI_CORRECT_END && ib == 0 && tid == 0) {
+                    L.ctl[sys].t += tau;
+                    L.ctl[sys].nsteps += 1;
+                }
             }
         }
-        __syncthreads();   // the records of this system are no longer read
+        // every thread read `item` before the copy barrier above, so the
+        // next item can be taken now; the barrier also ends this item's
+        // reads of the shared records before the next copy lands
+        if (tid == 0) item = atomicAdd(L.queue, 1u);
+        __syncthreads();
     }
 }
 
