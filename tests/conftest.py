@@ -15,8 +15,8 @@ def pytest_configure(config):
 
 def pytest_collection_modifyitems(config, items):
     # A GPU test must fail loudly on a machine with a GPU but without the
-    # library, but it
-    # cannot run at all where there is no GPU: only then is it skipped.
+    # library, but it cannot run at all where there is no GPU: only then is
+    # it skipped.
     try:
         import torch
         has_gpu = torch.cuda.is_available()
