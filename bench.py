@@ -370,19 +370,30 @@ def main():
     d2h = 8 * n * (3 + 6)
     e2e_val = world * inter / t_e2e / 1e9
 
-    # accuracy of this run's AccJerk against the oracle on an i-subset
+    # accuracy of this run's AccJerk against the fp64 EXACT sweep (the
+    # product's fp64 path, bit-identical to the reference's fp64 kernel) of
+    # an i-subset against all j
     acc_err = None
+    wa = None
+    idx = np.sort(np.random.default_rng(0).choice(n, 128, replace=False))
     if rank == 0:
-        import oracle
-        idx = np.sort(np.random.default_rng(0).choice(n, 128, replace=False))
-        sub = {k: np.ascontiguousarray(ps[k][idx]) for k in names8}
-        want = oracle.run("acc_jerk_kernel", sub, ps)
+        d_idx = torch.from_numpy(idx).to(dev)
+        d_sub = {k: d_in[k].index_select(0, d_idx).contiguous()
+                 for k in names8}
+        d_ex = [torch.empty(len(idx), dtype=torch.float64, device=dev)
+                for _ in range(6)]
+        lib.dev_sweep("acc_jerk_kernel", len(idx),
+                      [d_sub[k].data_ptr() for k in names8], n, p8,
+                      [t.data_ptr() for t in d_ex], mode=lib.MODE_EXACT,
+                      stream=sh)
+        torch.cuda.synchronize()
+        wa = np.stack([t.cpu().numpy() for t in d_ex[:3]])
         got = [t.cpu().numpy()[idx] for t in d_aj]
         ga = np.stack(got[:3])
-        wa = np.stack(want[:3])
         rel = np.linalg.norm(ga - wa, axis=0) / np.linalg.norm(wa, axis=0)
         acc_err = {"max": float(rel.max()), "median": float(np.median(rel)),
-                   "sample_i": int(len(idx))}
+                   "sample_i": int(len(idx)),
+                   "reference": "fp64 EXACT sweep of the same i against all j"}
 
     # --- the same sweeps with the Newton step after rsqrt (the variant the
     # default replaces: 9 -> 5, 10 -> 7, 11 -> 0), for comparison ----------
@@ -417,7 +428,7 @@ def main():
                   "acc_split_gints": n * n / (f0.elapsed_time(f1) / 1e3) / 1e9,
                   "acc_jerk_split_gints":
                       n * n / (f1.elapsed_time(f2) / 1e3) / 1e9,
-                  "acc_rel_err_vs_fp64_oracle": {
+                  "acc_rel_err_vs_fp64": {
                       "max": float(rel.max()),
                       "median": float(np.median(rel))}}
 
@@ -476,7 +487,7 @@ def main():
                     "fp64_exact_acc_jerk_gints": fp64_aj_gints,
                     "fp64_sample_ni": ni64,
                     "split_over_fp64": (inter / t_step) / (2.0 * ni64 * n / t64),
-                    "acc_rel_err_vs_fp64_oracle": acc_err,
+                    "acc_rel_err_vs_fp64": acc_err,
                     "newton_form": newton},
         "roofline": {"bound": "fp32",
                      "kernel": "split_sweep<AccJerkS> variant %d" % v_aj,

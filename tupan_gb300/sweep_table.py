@@ -1,7 +1,8 @@
 """Single force-evaluation sweeps at several N: Acc and AccJerk of all i
 against all j on equal-mass Plummer spheres (eps = 1e-4), SPLIT mode on the
 whole sphere and the fp64 EXACT mode on an i-subset, with the SPLIT error
-against the fp64 oracle on a random i-subset.
+against the fp64 EXACT sweep (bit-identical to the reference's fp64 kernel)
+on a random i-subset.
 
     python -m tupan_gb300.sweep_table --n 16384 65536 262144 1048576
 
@@ -30,7 +31,6 @@ def main(argv=None):
     a = ap.parse_args(argv)
 
     import torch
-    import oracle
     from . import ics, lib
 
     L = lib.load()
@@ -78,10 +78,20 @@ def main(argv=None):
                                      lib.MODE_EXACT))
         sweep("acc_jerk_kernel", n, p8, aj, lib.MODE_SPLIT)
         torch.cuda.synchronize()
+        # reference: the fp64 EXACT sweep (bit-identical to the reference's
+        # fp64 kernel) of a random i-subset against all j
         idx = np.sort(np.random.default_rng(0).choice(n, a.check_ni,
                                                       replace=False))
-        sub = {k: np.ascontiguousarray(ps[k][idx]) for k in names}
-        want = oracle.run("acc_jerk_kernel", sub, ps)
+        d_idx = torch.from_numpy(idx).cuda()
+        sub = [d[k].index_select(0, d_idx).contiguous() for k in names]
+        ex = [torch.empty(len(idx), dtype=torch.float64, device="cuda")
+              for _ in range(6)]
+        lib.dev_sweep("acc_jerk_kernel", len(idx),
+                      [t.data_ptr() for t in sub], n, p8,
+                      [t.data_ptr() for t in ex], mode=lib.MODE_EXACT,
+                      stream=stream.cuda_stream)
+        torch.cuda.synchronize()
+        want = [t.cpu().numpy() for t in ex]
         got = [t.cpu().numpy()[idx] for t in aj]
         ga, wa = np.stack(got[:3]), np.stack(want[:3])
         rel = np.linalg.norm(ga - wa, axis=0) / np.linalg.norm(wa, axis=0)
