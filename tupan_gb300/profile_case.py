@@ -5,6 +5,12 @@ acc_jerk_kernel --ni 77824 --nj 4194304 --mode split --reps 2``.
 Particles are a seeded Plummer sphere of nj bodies (the first ni are the
 i-particles).  Each repetition launches the library's sweep once; the time
 of each is printed with CUDA events.
+
+``--kernel hermite_step --nj N --order 4`` instead creates the device
+Hermite driver on N particles and takes `--reps` adaptive shared steps
+(each: Tstep sweep, state copy, forces, predictor, two forces + corrector
+passes), so the fp64 predictor and corrector can be profiled at sizes whose
+arrays exceed L2.
 """
 
 import argparse
@@ -22,7 +28,11 @@ def main(argv=None):
     ap.add_argument("--reps", type=int, default=2)
     ap.add_argument("--variant", type=int, default=-1)
     ap.add_argument("--gsplit", type=int, default=0)
+    ap.add_argument("--order", type=int, default=4)
     a = ap.parse_args(argv)
+
+    if a.kernel == "hermite_step":
+        return hermite_steps(a)
 
     import torch
     from . import abi, ics, lib
@@ -62,6 +72,24 @@ def main(argv=None):
                       "nj": a.nj, "times_s": times,
                       "gint_s": a.ni * a.nj / best / 1e9,
                       "variant": v, "gsplit": g}))
+
+
+def hermite_steps(a):
+    import time
+    from . import ics
+    from .integrator import DeviceHermite
+    ps = ics.plummer(a.nj, eps=1e-4, seed=3)
+    h = DeviceHermite(ps, 1.0 / 64, order=a.order, adaptive=True,
+                      mode=a.mode)
+    times = []
+    for k in range(a.reps):
+        t0 = time.perf_counter()
+        h.evolve(1.0, max_steps=1, batch=1)
+        times.append(time.perf_counter() - t0)
+    h.close()
+    print(json.dumps({"kernel": "hermite_step", "mode": a.mode,
+                      "n": a.nj, "order": a.order, "steps": a.reps,
+                      "times_s": times}))
 
 
 if __name__ == "__main__":
