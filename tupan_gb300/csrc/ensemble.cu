@@ -11,10 +11,13 @@
 // corrector) and packs the FP32 records the next sweep reads; only the
 // step size, a minimum over the whole system, waits for the system's last
 // item.  A step is a fixed sequence of five launches and `batch` steps are
-// captured in a CUDA graph and replayed.  A
-// run is usually dominated by a few systems with hard binaries that need
-// thousands of tiny shared steps, so the step latency with few active
-// systems is what the fused stages shorten.
+// captured in a CUDA graph and replayed.  Systems with hard binaries take
+// tens of thousands of small shared steps, so several hundred systems stay
+// active through most of a run: the sweep's throughput with a few hundred
+// mid-size systems (small CTAs, few barriers per item) sets the run time,
+// and the step latency once only a few systems remain sets its tail.
+// A persistent mode (k_e_run) instead gives each CTA a whole system for
+// many steps per launch.
 // Energies are fp64: an in-order fp64 Phi per system (same arithmetic and j
 // order as phi_kernel.c) and fp64 sums in fixed order.
 
