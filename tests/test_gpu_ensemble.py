@@ -94,3 +94,29 @@ def test_ensemble_set_mode_rejects_bad_arguments():
         with pytest.raises(lib.TupanGB300Error):
             ens.set_mode(*bad)
     ens.close()
+
+
+@pytest.mark.parametrize("mode", MODES)
+def test_ensemble_one_and_two_particle_systems(mode):
+    # a lone particle drifts; a pair is a two-body orbit; both next to a
+    # larger system
+    big = make_systems(1, lo=64, hi=64, seed=3)[0]
+    one = {k: np.ascontiguousarray(v[:1]) for k, v in big.items()}
+    two = {k: np.ascontiguousarray(v[1:3]) for k, v in big.items()}
+    systems = [big, one, two]
+    t_end, eta = 1.0 / 64, 1.0 / 64
+    ens = DeviceEnsemble(systems, eta)
+    ens.set_mode(*mode)
+    ens.evolve(t_end, batch=4)
+    t, k, st = ens.state()
+    assert np.all(t == t_end) and np.all(k >= 1)
+    off = ens.off
+    for s, ps in enumerate(systems):
+        ref = {c: v.copy() for c, v in ps.items()}
+        steps = oi.evolve(ref, t_end, eta, "ahermite4")
+        assert k[s] == len(steps), s
+        a, b = int(off[s]), int(off[s + 1])
+        for c in ("rx", "ry", "rz", "vx", "vy", "vz"):
+            scale = np.abs(ref[c]).max() + 1e-30
+            assert np.max(np.abs(st[c][a:b] - ref[c])) <= 1e-6 * scale, (s, c)
+    ens.close()

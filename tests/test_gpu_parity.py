@@ -271,6 +271,52 @@ def test_split_every_variant(variant, gsplit):
                                                         np.median(ej))
 
 
+def mixed_softening(n, seed):
+    """Plummer sphere whose per-particle e2 is uniform over the first 1024
+    particles and varies over the rest, so some j-tiles take the
+    per-tile softening shortcut and others form e2_i + e2_j per pair."""
+    ps = ics.plummer(n, eps=1e-4, seed=seed)
+    rng = np.random.default_rng(seed)
+    e2 = ps["e2"].copy()
+    e2[1024:] *= rng.uniform(0.25, 4.0, n - 1024)
+    ps["e2"] = e2
+    return ps
+
+
+@pytest.mark.parametrize("variant", [-1, 0, 5, 9, 10, 11])
+@pytest.mark.parametrize("name", ["phi_kernel", "acc_kernel",
+                                  "acc_jerk_kernel", "tstep_kernel",
+                                  "snap_crackle_kernel"])
+def test_split_mixed_softening(name, variant):
+    ps = mixed_softening(3000, 31)
+    if name == "snap_crackle_kernel":
+        aj = oracle.run("acc_jerk_kernel", ps, ps)
+        for c, k in zip(("ax", "ay", "az", "jx", "jy", "jz"), aj):
+            ps[c] = k
+    js = {k: np.ascontiguousarray(v[:2800]) for k, v in ps.items()}
+    sc = {"eta": 1.0 / 64} if name == "tstep_kernel" else None
+    want = oracle.run(name, ps, js, sc)
+    if variant >= 0:
+        lib.set_split_config(name, variant, 2)
+    try:
+        got = run_gpu(name, ps, js, sc, mode=lib.MODE_SPLIT)
+    finally:
+        lib.set_split_config(name, -1, 0)
+    if name == "phi_kernel":
+        err = np.abs(got[0] - want[0]) / np.abs(want[0])
+        assert err.max() <= 1e-6, err.max()
+    elif name in ("acc_kernel", "acc_jerk_kernel"):
+        err = vec_rel_err(got, want, (0, 1, 2))
+        assert err.max() <= 1e-6, err.max()
+    elif name == "tstep_kernel":
+        for g, w in zip(got, want):
+            assert np.max(np.abs(g - w) / w) <= 1e-5
+    else:
+        es = vec_rel_err(got, want, (0, 1, 2))
+        ec = vec_rel_err(got, want, (3, 4, 5))
+        assert np.median(es) <= 1e-5 and np.median(ec) <= 1e-5
+
+
 @pytest.mark.parametrize("variant", [9, 10, 11])
 @pytest.mark.parametrize("name", ["phi_kernel", "acc_kernel"])
 def test_split_no_newton_variants(name, variant):

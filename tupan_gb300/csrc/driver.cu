@@ -68,8 +68,9 @@ __device__ __forceinline__ double d_block_tstep(double min_ts, double t,
                                                 double tau)
 {
     // integrator/__init__.py:59-78 (power = int(log2(min_ts) - 1): C++'s
-    // conversion truncates toward zero like Python's int()).
-    long long power = (long long)(log2(min_ts) - 1.0);
+    // conversion truncates toward zero like Python's int(); the logarithm
+    // is exact at powers of two, see quantised_power).
+    long long power = quantised_power(min_ts);
     double min_bts = ldexp(1.0, (int)power);
     double t_next = t + min_bts;
     for (int k = 0; k < 2100 && fmod(t_next, min_bts) != 0.0; ++k)

@@ -65,7 +65,7 @@ __device__ __forceinline__ double e_base_tstep(double t, double t_end,
 __device__ __forceinline__ double e_block_tstep(double min_ts, double t,
                                                 double tau)
 {
-    long long power = (long long)(log2(min_ts) - 1.0);
+    long long power = quantised_power(min_ts);
     double min_bts = ldexp(1.0, (int)power);
     double t_next = t + min_bts;
     for (int k = 0; k < 2100 && fmod(t_next, min_bts) != 0.0; ++k)

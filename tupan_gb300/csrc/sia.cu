@@ -275,7 +275,7 @@ struct Frame {
 __device__ double d_block_tstep(double min_ts, double t, double tau)
 {
     // tupan/integrator/__init__.py:59-78
-    long long power = (long long)(log2(min_ts) - 1.0);
+    long long power = quantised_power(min_ts);
     double min_bts = ldexp(1.0, (int)power);
     const double t_next = t + min_bts;
     for (int k = 0; k < 2100 && fmod(t_next, min_bts) != 0.0; ++k)

@@ -16,6 +16,21 @@ namespace tg {
 // Kernels launched by this library since load (defined in abi.cu).
 extern std::atomic<unsigned long long> g_launch_count;
 
+// int(log2(min_ts) - 1), the exponent of tupan's power-of-two step
+// (integrator/__init__.py:59-78), as numpy evaluates it.  min_ts = m 2^e
+// exactly (frexp, m in [0.5, 1)); log2(2m) lies in [0, 1) and carries the
+// device log2's error only relative to that small value; the integer part
+// joins it in one rounding.  An exact power of two thus gives an exact
+// integer, as the host's log2 does: a log2 one ulp off there would make
+// the truncation pick a step twice as long.
+__device__ __forceinline__ long long quantised_power(double min_ts)
+{
+    int e;
+    const double m = frexp(min_ts, &e);
+    const double l = (double)(e - 1) + log2(2.0 * m);
+    return (long long)(l - 1.0);
+}
+
 
 // The ten entry points of tupan/lib/src/libtupan.h:2-246.
 enum KernelId : int {
