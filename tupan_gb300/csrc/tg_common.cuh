@@ -17,17 +17,21 @@ namespace tg {
 extern std::atomic<unsigned long long> g_launch_count;
 
 // int(log2(min_ts) - 1), the exponent of tupan's power-of-two step
-// (integrator/__init__.py:59-78), as numpy evaluates it.  min_ts = m 2^e
-// exactly (frexp, m in [0.5, 1)); log2(2m) lies in [0, 1) and carries the
-// device log2's error only relative to that small value; the integer part
-// joins it in one rounding.  An exact power of two thus gives an exact
-// integer, as the host's log2 does: a log2 one ulp off there would make
-// the truncation pick a step twice as long.
+// (integrator/__init__.py:59-78), as numpy evaluates it with a correctly
+// rounded log2.  min_ts = m 2^e exactly (frexp, m in [0.5, 1)); the
+// logarithm is taken of whichever of m and 2m lies in [sqrt(1/2), sqrt(2)),
+// so near a power of two, where the truncation is decided, it is a value
+// near zero whose absolute error is negligible, and the integer part joins
+// it in one rounding.  The device log2 of min_ts itself is one ulp off at
+// exact powers of two, which the truncation turns into a step twice as
+// long.
 __device__ __forceinline__ long long quantised_power(double min_ts)
 {
     int e;
     const double m = frexp(min_ts, &e);
-    const double l = (double)(e - 1) + log2(2.0 * m);
+    const double l = m < 0.70710678118654752
+                         ? (double)(e - 1) + log2(2.0 * m)
+                         : (double)e + log2(m);
     return (long long)(l - 1.0);
 }
 
