@@ -664,13 +664,6 @@ struct Ensemble {
     unsigned switch_below = 0;      // persistent -> batched below this many
 };
 
-unsigned grid_for(uint64_t n, int sms)
-{
-    uint64_t b = (n + 255) / 256;
-    uint64_t cap = (uint64_t)sms * 8;
-    return (unsigned)(b < 1 ? 1 : (b > cap ? cap : b));
-}
-
 // One force evaluation of every active system from the current records,
 // followed per system by the epilogue `epi`.
 cudaError_t e_sweep(Ensemble *E, int kernel, double *const *out, double eta,
