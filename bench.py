@@ -149,20 +149,35 @@ def roofline_traffic():
     return None
 
 
-def cpu_baseline(n, ni, ps):
+def cpu_baseline(n, ni, ps, single_ni=None):
     """Oracle (bit-identical restatement of the reference C kernels) on all
-    host threads over ni i-particles x all n j-particles, both kernels."""
+    host threads over ni i-particles x all n j-particles, both kernels; and
+    on one thread, as the reference ships (single-threaded C), over
+    single_ni i-particles (default ni / 16, about the same wall time)."""
     import oracle
     threads = oracle.max_threads()
-    sub = {k: np.ascontiguousarray(v[:ni]) for k, v in ps.items()}
-    t0 = time.perf_counter()
-    oracle.run("acc_kernel", sub, ps)
-    oracle.run("acc_jerk_kernel", sub, ps)
-    dt = time.perf_counter() - t0
+
+    def timed(k):
+        sub = {a: np.ascontiguousarray(v[:k]) for a, v in ps.items()}
+        t0 = time.perf_counter()
+        oracle.run("acc_kernel", sub, ps)
+        oracle.run("acc_jerk_kernel", sub, ps)
+        return time.perf_counter() - t0
+
+    dt = timed(ni)
+    k1 = max(1, single_ni if single_ni is not None else ni // 16)
+    oracle.set_threads(1)
+    try:
+        dt1 = timed(k1)
+    finally:
+        oracle.set_threads(threads)
     return {"value": 2.0 * ni * n / dt / 1e9, "unit": "Gint/s",
             "cores": threads, "kind": "port",
             "sample": "acc + acc_jerk, ni=%d x nj=%d of the N=%d Plummer "
-                      "sphere (%.1f s)" % (ni, n, n, dt)}
+                      "sphere (%.1f s)" % (ni, n, n, dt),
+            "single_core": {"value": 2.0 * k1 * n / dt1 / 1e9,
+                            "unit": "Gint/s", "cores": 1,
+                            "sample": "ni=%d x nj=%d (%.1f s)" % (k1, n, dt1)}}
 
 
 def kepler_solves(torch, stream):
