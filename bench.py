@@ -149,6 +149,16 @@ def roofline_traffic():
     return None
 
 
+def achieved_aj(n, t_aj):
+    """AccJerk TFLOP/s at the reference's 42 flop per interaction."""
+    return n * n * FLOPS_ACC_JERK / t_aj / 1e12
+
+
+def nominal_fp32_tflops(sms, sm_mhz):
+    """SMs x 128 FP32 lanes x 2 flop per FMA x SM clock, in TFLOP/s."""
+    return sms * 128 * 2 * sm_mhz * 1e6 / 1e12
+
+
 def cpu_baseline(n, ni, ps, single_ni=None):
     """Oracle (bit-identical restatement of the reference C kernels) on all
     host threads over ni i-particles x all n j-particles, both kernels; and
@@ -472,6 +482,18 @@ def main():
     peak.tupan_gb300_fp32_peak_tflops.restype = ctypes.c_double
     peak.tupan_gb300_fp32_peak_tflops.argtypes = [ctypes.c_int, ctypes.c_int]
     fp32_peak = float(peak.tupan_gb300_fp32_peak_tflops(20000, 5))
+    # the same peak derived from the SM count and the SM clock sampled under
+    # load, as a cross-check of the measured one
+    nominal = None
+    try:
+        sms = torch.cuda.get_device_properties(dev).multi_processor_count
+        mhz = float(clk.get("sm_mhz") or clk.get("sm_max_mhz"))
+        tf = nominal_fp32_tflops(sms, mhz)
+        nominal = {"value": tf, "unit": "TFLOP/s", "sms": sms,
+                   "sm_mhz": mhz, "frac": achieved_aj(n, t_aj) / tf,
+                   "formula": "SMs x 128 lanes x 2 flop x SM clock"}
+    except Exception:
+        nominal = None
 
 
     kepler = kepler_solves(torch, stream) if rank == 0 else None
@@ -512,6 +534,7 @@ def main():
                      "peak_source": "FP32 FMA-chain kernel measured in this "
                                     "run (MEASURED_PEAKS.json has no FP32 "
                                     "figure)",
+                     "peak_nominal": nominal,
                      "traffic": traffic},
         "cpu_baseline": cpu,
         "e2e": {"value": e2e_val, "unit": "Gint/s",

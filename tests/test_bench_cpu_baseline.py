@@ -23,3 +23,10 @@ def test_cpu_baseline_reports_all_threads_and_one():
     one = out["single_core"]
     assert one["cores"] == 1 and one["value"] > 0
     assert "ni=16 x nj=2048" in one["sample"]
+
+
+def test_nominal_fp32_peak_formula():
+    # 152 SMs x 128 lanes x 2 flop x 2070 MHz
+    assert abs(bench.nominal_fp32_tflops(152, 2070.0) - 80.54784) < 1e-9
+    # 262144^2 interactions x 42 flop in 77.2 ms
+    assert abs(bench.achieved_aj(262144, 0.0772) - 37.3862) < 1e-3
