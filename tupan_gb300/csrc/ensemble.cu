@@ -435,8 +435,13 @@ k_e_sweep(const BatchLaunch L)
             bulk_g2s(rec, L.rec + b * NF, bytes, &bar);
         }
         bool got = mbar_wait_bounded(&bar, phase, L.err);
+        if (!__syncthreads_and(got)) {
+            // the copy did not complete in time: wait (bounded) once more
+            // for it before the shared memory goes away, then leave
+            if (tid == 0) mbar_wait_bounded(&bar, phase, L.err);
+            break;
+        }
         phase ^= 1u;
-        if (!__syncthreads_and(got)) break;
         const uint64_t bi = b + ib, ei = b + ie;
         // Tstep sweeps (the one operator with a max output) end in the
         // step size; AccJerk sweeps in the predictor or corrector
