@@ -178,11 +178,11 @@ split_sweep(const SplitLaunch L)
             }
     };
 
-    int failed = -1;                 // tile whose copy did not complete
+    bool ok = true;
     for (int t = 0; t < ntiles; ++t) {
         bool got = mbar_wait_bounded(&bar[t & 1], (uint32_t)((t >> 1) & 1),
                                      L.err);
-        if (!__syncthreads_and(got)) { failed = t; break; }
+        if (!__syncthreads_and(got)) { ok = false; break; }
         const float4 *tile = &ring[t & 1][0];
         const uint64_t j0 = jb + (uint64_t)t * TJ;
         const int n = (int)((je - j0) < (uint64_t)TJ ? (je - j0) : TJ);
@@ -285,15 +285,16 @@ split_sweep(const SplitLaunch L)
         __syncthreads();
         if (tid == 0 && t + 2 < ntiles) issue(t + 2);
     }
-    if (failed >= 0) {
-        // A copy did not complete in time: wait (bounded) for the copies
-        // still in flight -- the failed tile's and the next one's, which was
-        // issued with it -- before the shared memory goes away, then leave
-        // without writing results (the host reports the error word).
+    if (!ok) {
+        // A copy did not complete in time: wait (bounded) for whatever is
+        // still in flight before the shared memory goes away, then leave
+        // without writing results (the host reports the error word).  Each
+        // slot is waited on with both parities: the completed one returns
+        // at once, the pending one (if any) waits for its copy.
         if (tid == 0)
-            for (int t = failed; t < failed + 2 && t < ntiles; ++t)
-                mbar_wait_bounded(&bar[t & 1], (uint32_t)((t >> 1) & 1),
-                                  L.err);
+            for (int s = 0; s < 2; ++s)
+                for (uint32_t p = 0; p < 2; ++p)
+                    mbar_wait_bounded(&bar[s], p, L.err);
         return;
     }
 
