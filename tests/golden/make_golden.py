@@ -271,6 +271,58 @@ def integrators(refroot):
     print("wrote", fn, os.path.getsize(fn))
 
 
+TINY_RUNS = [
+    # (method, first, last particle of a 64-body Plummer sphere, eta, t_end)
+    # a lone particle's step is eta exactly, a power of two, where the step
+    # quantisation's truncation is decided by the last bit of log2
+    ("ahermite4", 0, 1, 1.0 / 64, 1.0 / 16),
+    ("ahermite4", 1, 3, 1.0 / 64, 1.0 / 16),
+    ("ahermite6", 0, 1, 1.0 / 32, 1.0 / 8),
+    ("ahermite6", 1, 3, 1.0 / 32, 1.0 / 8),
+]
+
+
+def tiny(refroot):
+    """Runs of the reference's own integrators on 1- and 2-particle systems
+    (tupan/integrator/__init__.py:59-78 quantises a lone particle's step
+    eta to eta / 2)."""
+    sys.path.insert(0, refroot)
+    sys.path.insert(0, os.path.dirname(os.path.dirname(HERE)))
+    from tupan.integrator import Integrator
+    from tupan.particles.allparticles import ParticleSystem
+    from tupan_gb300 import ics
+
+    d = ics.plummer(64, eps=1e-4, seed=3)
+    store = {}
+    for k, (method, lo, hi, eta, t_end) in enumerate(TINY_RUNS):
+        n = hi - lo
+        ps = ParticleSystem(n)
+        ps.mass[...] = d["m"][lo:hi]
+        ps.eps2[...] = d["e2"][lo:hi]
+        for a in ("rx", "ry", "rz", "vx", "vy", "vz"):
+            getattr(ps, a)[...] = d[a][lo:hi]
+        tag = "%d/" % k
+        for a in ("m", "e2", "rx", "ry", "rz", "vx", "vy", "vz"):
+            store[tag + "in/" + a] = d[a][lo:hi].copy()
+        integ = Integrator(eta, 0.0, ps, method=method)
+        steps = []
+        while abs(integ.time) < t_end:
+            t0 = integ.time
+            integ.evolve_step(t_end)
+            steps.append(integ.time - t0)
+        ps = integ.particle_system
+        store[tag + "method"] = np.array(method)
+        store[tag + "params"] = np.array([eta, t_end])
+        store[tag + "steps"] = np.array(steps)
+        for a in ("rx", "ry", "rz", "vx", "vy", "vz"):
+            store[tag + "out/" + a] = np.array(getattr(ps, a), copy=True)
+        print(method, n, "particles:", len(steps), "steps of", steps[0])
+    store["runs"] = np.array(len(TINY_RUNS))
+    fn = os.path.join(HERE, "golden_tiny.npz")
+    np.savez_compressed(fn, **store)
+    print("wrote", fn, os.path.getsize(fn))
+
+
 def config1(refroot):
     """The CPU-runnable configuration in full: Plummer N=256, equal masses,
     eps=1e-4, tupan's ahermite4 (shared adaptive steps, eta=1/64) to
@@ -465,6 +517,8 @@ if __name__ == "__main__":
         nreg(ref)
     elif "--plummer" in sys.argv:
         plummer(ref)
+    elif "--tiny" in sys.argv:
+        tiny(ref)
     else:
         main(ref)
         integrators(ref)
@@ -472,3 +526,4 @@ if __name__ == "__main__":
         config1(ref)
         nreg(ref)
         plummer(ref)
+        tiny(ref)

@@ -44,6 +44,22 @@ def test_exact_hermite_bit_identical_to_reference(method, batch):
     h.close()
 
 
+@pytest.mark.parametrize("batch", [1, 4])
+def test_exact_hermite_tiny_systems_bit_identical_to_reference(batch):
+    # 1- and 2-particle systems (golden_tiny.npz): a lone particle's step is
+    # eta exactly, a power of two that the quantisation halves
+    from tests.test_oracle_tiny import tiny_runs
+    for method, ps, eta, t_end, steps, out in tiny_runs():
+        h = DeviceHermite(ps, eta, order=ORDER[method], adaptive=True,
+                          mode="exact", record_steps=1000)
+        h.evolve(t_end, batch=batch)
+        np.testing.assert_array_equal(h.steps(), steps)
+        got = h.state()
+        for k, v in out.items():
+            np.testing.assert_array_equal(got[k], v)
+        h.close()
+
+
 def test_split_hermite4_energy_and_steps():
     # Config 1 shape (Plummer, eta = 1/64, eps = 1e-4) over a short time.
     # The energy diagnostic is fp64; SPLIT forces add FP32 force noise, so
