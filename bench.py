@@ -247,26 +247,55 @@ def kepler_solves(torch, stream):
     return res
 
 
+def reference_step(ps, sub):
+    """One Acc + AccJerk sweep of the i-subset `sub` against all of `ps` on
+    the host: the reference kernels compiled from their own sources
+    (oracle/_ref, single-threaded C as shipped) fanned out over i-ranges on
+    every host thread where they are built, else the oracle port (the same
+    arithmetic bit for bit) on its own threads.  Returns (step, kind,
+    threads)."""
+    import oracle
+    threads = oracle.max_threads()
+    if not oracle.ref_available():
+        def step():
+            oracle.run("acc_kernel", sub, ps)
+            oracle.run("acc_jerk_kernel", sub, ps)
+        return step, "port", threads
+    from concurrent.futures import ThreadPoolExecutor
+    ni = len(sub["m"])
+    cuts = np.linspace(0, ni, threads + 1).astype(int)
+    chunks = [{k: np.ascontiguousarray(v[a:b]) for k, v in sub.items()}
+              for a, b in zip(cuts[:-1], cuts[1:]) if b > a]
+    pool = ThreadPoolExecutor(max_workers=len(chunks))
+
+    def step():
+        # ctypes releases the GIL for the duration of each C call
+        jobs = [pool.submit(oracle.run_ref, name, c, ps)
+                for name in ("acc_kernel", "acc_jerk_kernel") for c in chunks]
+        for j in jobs:
+            j.result()
+    return step, "reference", len(chunks)
+
+
 def run_reference(args):
-    """--impl reference: the reference kernels' CPU path (the oracle port,
-    bit-identical to tupan's C backend) on all host threads."""
+    """--impl reference: the reference kernels' CPU path on all host
+    threads (reference_step)."""
     rank, world, local = dist_env()
     if rank != 0:
         return
     from tupan_gb300 import ics
-    import oracle
     n = args.n
     ps = ics.plummer(n, eps=1e-4, seed=1)
     ni = args.cpu_ni
     sub = {k: np.ascontiguousarray(v[:ni]) for k, v in ps.items()}
-    threads = oracle.max_threads()
-    for _ in range(max(1, args.warmup) if False else 1):
-        oracle.run("acc_kernel", {k: v[:64].copy() for k, v in sub.items()}, ps)
+    step, kind, threads = reference_step(ps, sub)
+    warm, _, _ = reference_step(
+        ps, {k: np.ascontiguousarray(v[:64]) for k, v in sub.items()})
+    warm()
     times = []
     for _ in range(args.steps):
         t0 = time.perf_counter()
-        oracle.run("acc_kernel", sub, ps)
-        oracle.run("acc_jerk_kernel", sub, ps)
+        step()
         times.append(time.perf_counter() - t0)
     t = float(np.mean(times))
     val = 2.0 * ni * n / t / 1e9
@@ -279,7 +308,7 @@ def run_reference(args):
                                    % n, "sample_ni": ni, "n": n},
             "impl": "reference",
             "cpu_baseline": {"value": val, "unit": "Gint/s", "cores": threads,
-                             "kind": "port",
+                             "kind": kind,
                              "sample": "ni=%d x nj=%d per step" % (ni, n)},
             "e2e": {"value": val, "unit": "Gint/s", "h2d_bytes_per_step": 0,
                     "d2h_bytes_per_step": 0}}
