@@ -4,7 +4,8 @@
 //  * Positions are split once per call into hi + lo floats (pack kernel), so
 //    x_j - x_i is formed as (xh_j - xh_i) + (xl_j - xl_i): the difference of
 //    two nearby positions keeps ~48 bits instead of FP32's 24.
-//  * 1/sqrt(r^2 + eps^2) is rsqrt (MUFU) plus one Newton step.
+//  * 1/sqrt(r^2 + eps^2) is the MUFU rsqrt alone (variants 9-11, the
+//    default) or rsqrt plus one Newton step (variants 0-8).
 //  * Each lane sums a run of pair terms in FP32, then folds the run into a
 //    Kahan-compensated (sum, correction) pair; the final value is formed in
 //    double.  j-split lanes of one i are combined with warp shuffles, grid
