@@ -185,6 +185,13 @@ int tupan_gb300_split_variants(void);
 void tupan_gb300_split_variant_info(int variant, int *ni_per_thread,
                                     int *jsplit, int *threads);
 
+/* Tries of each main-loop wait of the pipelined sweeps on its copy barrier
+ * before the CTA records device error bit 0 and leaves without writing
+ * results (default 2^20; 0 makes every such wait time out at once, for
+ * testing the error path).  The waits that drain copies still in flight keep
+ * the full bound.  Returns the previous limit. */
+unsigned tupan_gb300_set_pipe_spin_limit(unsigned limit);
+
 /* One sweep over DEVICE arrays.  i_attrs / j_attrs: host arrays holding the
  * device pointers of the kernel's per-particle inputs in libtupan.h order
  * (j_attrs unused for Kepler); outs: device pointers of its outputs.

@@ -63,6 +63,8 @@ int split_nf_host(int kernel);
 
 namespace tg {
 std::atomic<unsigned long long> g_launch_count{0};
+std::atomic<uint32_t> g_pipe_spin{1u << 20};
+uint32_t pipe_spin_limit() { return g_pipe_spin.load(); }
 }
 
 using namespace tg;
@@ -759,6 +761,15 @@ TG_EXPORT int tupan_gb300_split_choice(int kernel, uint64_t ni, uint64_t nj,
     if (rc) return rc;
     choose_split(d, kernel, ni, nj, variant, gsplit);
     return ST_OK;
+}
+
+// Tries each main-loop wait of the pipelined sweeps (split, centred,
+// ensemble) makes on its copy barrier before it records DERR_PIPE_TIMEOUT
+// and the CTA leaves without writing results (default 2^20; 0 makes every
+// such wait time out at once).  Returns the previous limit.
+TG_EXPORT unsigned tupan_gb300_set_pipe_spin_limit(unsigned limit)
+{
+    return g_pipe_spin.exchange(limit);
 }
 
 // Variants of the SPLIT sweep (0..8, compiled for every SPLIT kernel).

@@ -291,6 +291,7 @@ struct BatchLaunch {
     float eta;
     double eta_d;
     unsigned *err;
+    uint32_t spin;            // main-loop wait limit (pipe_spin_limit())
     int epi;
     EArrays A;
     SysCtl *ctl;
@@ -434,7 +435,7 @@ k_e_sweep(const BatchLaunch L)
             mbar_arrive_expect_tx(&bar, bytes);
             bulk_g2s(rec, L.rec + b * NF, bytes, &bar);
         }
-        bool got = mbar_wait_bounded(&bar, phase, L.err);
+        bool got = mbar_wait_bounded(&bar, phase, L.err, L.spin);
         if (!__syncthreads_and(got)) {
             // the copy did not complete in time: wait (bounded) once more
             // for it before the shared memory goes away, then leave
@@ -687,6 +688,7 @@ cudaError_t e_sweep(Ensemble *E, int kernel, double *const *out, double eta,
     L.eta = (float)eta;
     L.eta_d = eta;
     L.err = E->err;
+    L.spin = pipe_spin_limit();   // read when a step is launched or captured
     L.epi = epi;
     L.A = E->A;
     L.ctl = E->ctl;

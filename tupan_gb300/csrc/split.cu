@@ -92,6 +92,7 @@ struct SplitLaunch {
     float eta;
     double eta_d;
     unsigned *err;
+    uint32_t spin;        // main-loop wait limit (pipe_spin_limit())
 };
 
 constexpr int SPLIT_TILE = 256;   // j-records per pipeline stage
@@ -180,10 +181,11 @@ split_sweep(const SplitLaunch L)
     };
 
     bool ok = true;
+    int tfail = 0;
     for (int t = 0; t < ntiles; ++t) {
         bool got = mbar_wait_bounded(&bar[t & 1], (uint32_t)((t >> 1) & 1),
-                                     L.err);
-        if (!__syncthreads_and(got)) { ok = false; break; }
+                                     L.err, L.spin);
+        if (!__syncthreads_and(got)) { ok = false; tfail = t; break; }
         const float4 *tile = &ring[t & 1][0];
         const uint64_t j0 = jb + (uint64_t)t * TJ;
         const int n = (int)((je - j0) < (uint64_t)TJ ? (je - j0) : TJ);
@@ -287,15 +289,14 @@ split_sweep(const SplitLaunch L)
         if (tid == 0 && t + 2 < ntiles) issue(t + 2);
     }
     if (!ok) {
-        // A copy did not complete in time: wait (bounded) for whatever is
-        // still in flight before the shared memory goes away, then leave
-        // without writing results (the host reports the error word).  Each
-        // slot is waited on with both parities: the completed one returns
-        // at once, the pending one (if any) waits for its copy.
+        // A copy did not complete in time.  The copies of tiles tfail and
+        // tfail + 1 (where they exist) were issued and not yet consumed:
+        // wait for each (full bound, its pending parity) before the shared
+        // memory goes away, then leave without writing results (the host
+        // reports the error word).
         if (tid == 0)
-            for (int s = 0; s < 2; ++s)
-                for (uint32_t p = 0; p < 2; ++p)
-                    mbar_wait_bounded(&bar[s], p, L.err);
+            for (int u = tfail; u < ntiles && u < tfail + 2; ++u)
+                mbar_wait_bounded(&bar[u & 1], (uint32_t)((u >> 1) & 1), L.err);
         return;
     }
 
@@ -345,6 +346,8 @@ template <class Op>
 __global__ void split_finalize(const SplitLaunch L, int gsplit)
 {
     constexpr int NO = Op::NO, MAXC = Op::MAXC;
+    // a sweep CTA that reported an error left its partials unwritten
+    if (*(volatile unsigned *)L.err) return;
     for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
          i < L.ni; i += (uint64_t)gridDim.x * blockDim.x) {
         double v[NO];
@@ -508,6 +511,7 @@ cudaError_t launch_split(int kernel, const float4 *irec, const float4 *jrec,
     L.eta = (float)eta;
     L.eta_d = eta;
     L.err = err;
+    L.spin = pipe_spin_limit();
     switch (kernel) {
     case K_PHI: return run_op<PhiS>(L, variant, gsplit, st);
     case K_ACC: return run_op<AccS>(L, variant, gsplit, st);

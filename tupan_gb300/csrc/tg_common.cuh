@@ -16,6 +16,10 @@ namespace tg {
 // Kernels launched by this library since load (defined in abi.cu).
 extern std::atomic<unsigned long long> g_launch_count;
 
+// Tries a sweep's main-loop pipeline wait makes before it reports
+// DERR_PIPE_TIMEOUT (defined in abi.cu; tupan_gb300_set_pipe_spin_limit).
+uint32_t pipe_spin_limit();
+
 // int(log2(min_ts) - 1), the exponent of tupan's power-of-two step
 // (integrator/__init__.py:59-78), as numpy evaluates it with a correctly
 // rounded log2.  min_ts = m 2^e exactly (frexp, m in [0.5, 1)); the

@@ -61,12 +61,17 @@ __device__ __forceinline__ bool mbar_try_wait(uint64_t *bar, uint32_t parity)
 constexpr uint32_t MBAR_SPIN_LIMIT = 1u << 20;
 
 // Returns false (and records DERR_PIPE_TIMEOUT) if the phase did not
-// complete within the spin limit.
+// complete within `limit` tries (MBAR_SPIN_LIMIT by default).  The sweeps'
+// main-loop waits take the limit from their launch descriptor
+// (pipe_spin_limit(), settable from the host) so that the timeout path can
+// be exercised; the waits that drain copies still in flight before a CTA
+// returns always use the full bound.
 __device__ __forceinline__ bool mbar_wait_bounded(uint64_t *bar,
                                                   uint32_t parity,
-                                                  unsigned *err)
+                                                  unsigned *err,
+                                                  uint32_t limit = MBAR_SPIN_LIMIT)
 {
-    for (uint32_t k = 0; k < MBAR_SPIN_LIMIT; ++k)
+    for (uint32_t k = 0; k < limit; ++k)
         if (mbar_try_wait(bar, parity)) return true;
     atomicOr(err, (unsigned)DERR_PIPE_TIMEOUT);
     return false;

@@ -69,6 +69,8 @@ def _declare(L):
     L.tupan_gb300_kernel_arity.restype = c.c_int
     L.tupan_gb300_device_sms.restype = c.c_int
     L.tupan_gb300_real_bits.restype = c.c_int
+    L.tupan_gb300_set_pipe_spin_limit.argtypes = [c.c_uint]
+    L.tupan_gb300_set_pipe_spin_limit.restype = c.c_uint
 
 
 def load(prec="float64"):
@@ -132,6 +134,12 @@ def split_variants():
         out.append({"ni_per_thread": a.value, "jsplit": b.value,
                     "threads": c.value})
     return out
+
+
+def set_pipe_spin_limit(limit, prec="float64"):
+    """Tries of each main-loop copy-barrier wait before DERR_PIPE_TIMEOUT
+    (default 2**20); returns the previous limit."""
+    return load(prec).tupan_gb300_set_pipe_spin_limit(int(limit))
 
 
 def set_split_config(kernel, variant, gsplit=1):
