@@ -185,6 +185,17 @@ int tupan_gb300_split_variants(void);
 void tupan_gb300_split_variant_info(int variant, int *ni_per_thread,
                                     int *jsplit, int *threads);
 
+/* Centred SPLIT sweeps of phi, acc and acc_jerk: particles in Morton order,
+ * j-tiles stored relative to their centre, a one-operation position
+ * difference for tiles far from every i of a warp.  policy -1: automatic
+ * (sweeps of at least 2^28 interactions), 0: never, 1: always; shape (i per
+ * thread: 0 = one, 1 = two) and grid j-split gsplit: < 0 / <= 0 automatic.
+ * Returns 0 or 2 (bad argument). */
+int tupan_gb300_set_centred(int policy, int shape, int gsplit);
+/* The path a SPLIT sweep of this size takes: *path 1 = centred (*config =
+ * shape), 0 = split variants (*config = variant); *gsplit = grid j-split. */
+int tupan_gb300_sweep_plan(int kernel, uint64_t ni, uint64_t nj, int *path,
+                           int *config, int *gsplit);
 /* Tries of each main-loop wait of the pipelined sweeps on its copy barrier
  * before the CTA records device error bit 0 and leaves without writing
  * results (default 2^20; 0 makes every such wait time out at once, for

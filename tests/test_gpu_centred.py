@@ -1,0 +1,186 @@
+"""Centred SPLIT sweeps (csweep.cu) against the fp64 oracle.
+
+The centred path Morton-orders the particles, stores each 256-particle
+j-tile relative to its centre and takes a one-operation position difference
+for tiles far from every i of a warp.  These tests force it on
+(``set_centred(1)``) at sizes where the automatic choice would not take it,
+and run it at the configurations' own sizes, where it is the default.
+
+Bounds per particle against the oracle (the reference's fp64 arithmetic):
+  * at the configuration sizes (N = 262144 and 1048576; the lowest-|a|
+    particles at the sphere's centre and random ones): |da|/|a| <= 1e-6;
+  * on small spheres: median |da|/|a| <= 1e-7 and max <= 2e-6.  FP32 pair
+    arithmetic reaches about 1.2e-6 on rare particles whose net force is a
+    near-cancelling sum with one close pair several times larger (measured on
+    N = 3000, seed 12: the double-single split path 1.20e-6, the centred
+    path 1.15e-6 on the same particle), so the tight bound is the median;
+  * jerk: median <= 1e-6 and max <= 1e-4; phi: max <= 1e-6.
+"""
+
+import numpy as np
+import pytest
+
+import oracle
+from tupan_gb300 import abi, ics, lib
+
+pytestmark = pytest.mark.gpu
+
+KERNELS = ("phi_kernel", "acc_kernel", "acc_jerk_kernel")
+
+
+def run_centred(name, ips, jps, policy=1, shape=-1, gsplit=0):
+    lib.set_centred(policy, shape, gsplit)
+    old = lib.set_mode(lib.MODE_SPLIT)
+    try:
+        fn = lib.bind(name)
+        vals = abi.make_args(name, "float64", ips, jps)
+        abi.call(fn, name, "float64", vals)
+        lib.check()
+        return abi.outputs(name, vals)
+    finally:
+        lib.set_mode(old)
+        lib.set_centred(-1, -1, 0)
+
+
+def vec_rel_err(got, want, comps):
+    g = np.stack([got[c] for c in comps])
+    w = np.stack([want[c] for c in comps])
+    return np.linalg.norm(g - w, axis=0) / np.linalg.norm(w, axis=0)
+
+
+def assert_bounds(name, got, want, amax=2e-6):
+    assert all(np.all(np.isfinite(g)) for g in got), name
+    if name == "phi_kernel":
+        e = np.abs(got[0] - want[0]) / np.abs(want[0])
+        assert e.max() <= 1e-6, (name, e.max())
+        return
+    ea = vec_rel_err(got, want, (0, 1, 2))
+    assert np.median(ea) <= 1e-7 and ea.max() <= amax, (
+        name, ea.max(), np.median(ea))
+    if name == "acc_jerk_kernel":
+        ej = vec_rel_err(got, want, (3, 4, 5))
+        assert np.median(ej) <= 1e-6 and ej.max() <= 1e-4, (ej.max(),
+                                                            np.median(ej))
+
+
+def sub(ps, idx):
+    return {k: np.ascontiguousarray(v[idx]) for k, v in ps.items()}
+
+
+@pytest.mark.parametrize("shape", [0, 1])
+@pytest.mark.parametrize("n", [1000, 4096, 20000])
+@pytest.mark.parametrize("name", KERNELS)
+def test_centred_accuracy(name, n, shape):
+    ps = ics.plummer(n, eps=1e-4, seed=n + 3)
+    want = oracle.run(name, ps, ps)
+    got = run_centred(name, ps, ps, shape=shape)
+    assert_bounds(name, got, want)
+
+
+@pytest.mark.parametrize("gsplit", [1, 2, 5, 64])
+def test_centred_grid_splits(gsplit):
+    ps = ics.plummer(6000, eps=1e-4, seed=77)
+    js = sub(ps, slice(0, 5500))
+    for name in KERNELS:
+        want = oracle.run(name, ps, js)
+        got = run_centred(name, ps, js, gsplit=gsplit)
+        assert_bounds(name, got, want)
+
+
+@pytest.mark.parametrize("ni,nj", [(1, 1), (1, 5000), (5000, 1), (7, 300),
+                                   (513, 257), (300, 3), (2049, 4097)])
+def test_centred_edge_sizes(ni, nj):
+    # disjoint i and j sets (no aliasing): each is sorted on its own
+    ps = ics.plummer(ni + nj, eps=1e-4, seed=ni * 7 + nj)
+    ip = sub(ps, slice(0, ni))
+    jp = sub(ps, slice(ni, ni + nj))
+    for name in KERNELS:
+        want = oracle.run(name, ip, jp)
+        got = run_centred(name, ip, jp)
+        assert all(np.all(np.isfinite(g)) for g in got), name
+        for g, w in zip(got, want):
+            scale = np.abs(w).max() + 1e-300
+            assert np.max(np.abs(g - w)) <= 1e-5 * scale, name
+
+
+def test_centred_unsoftened_self_and_coincident_pairs():
+    # eps2 = 0 and every position present twice (at other indices): the
+    # r2 > 0 mask must remove self pairs and coincident pairs, whichever
+    # tiles they land in, without producing inf or NaN.
+    rng = np.random.default_rng(4)
+    n = 2000
+    base = {k: rng.random(n) * 10 for k in ("rx", "ry", "rz",
+                                             "vx", "vy", "vz")}
+    base["m"] = rng.random(n)
+    base["e2"] = np.zeros(n)
+    perm = rng.permutation(2 * n)
+    ps = {k: np.ascontiguousarray(np.concatenate([v, v])[perm])
+          for k, v in base.items()}
+    for name in KERNELS:
+        want = oracle.run(name, ps, ps)
+        got = run_centred(name, ps, ps)
+        assert all(np.all(np.isfinite(g)) for g in got), name
+        comps = (0,) if name == "phi_kernel" else (0, 1, 2)
+        e = vec_rel_err(got, want, comps)
+        assert e.max() <= 1e-5, (name, e.max())
+
+
+def test_centred_mixed_softening():
+    # per-particle softening that varies over most particles: tiles without
+    # one common e2 form e2_i + e2_j per pair
+    ps = ics.plummer(5000, eps=1e-4, seed=31)
+    rng = np.random.default_rng(31)
+    ps["e2"] = ps["e2"].copy()
+    ps["e2"][1024:] *= rng.uniform(0.25, 4.0, 5000 - 1024)
+    for name in KERNELS:
+        want = oracle.run(name, ps, ps)
+        got = run_centred(name, ps, ps)
+        assert_bounds(name, got, want)
+
+
+def test_centred_matches_split_variants():
+    # the same sweep through both SPLIT paths agrees within their bounds
+    ps = ics.plummer(8192, eps=1e-4, seed=8)
+    for name in KERNELS:
+        a = run_centred(name, ps, ps, policy=1)
+        b = run_centred(name, ps, ps, policy=0)
+        comps = (0,) if name == "phi_kernel" else (0, 1, 2)
+        e = vec_rel_err(a, b, comps)
+        assert e.max() <= 2e-6 and np.median(e) <= 1e-7, name
+
+
+def worst_and_random(ps, n, k, seed):
+    """The k lowest-|a| particles (the Plummer centre, where |a| is a
+    near-cancelling sum) and k random others."""
+    r2 = ps["rx"] ** 2 + ps["ry"] ** 2 + ps["rz"] ** 2
+    low = np.argsort(r2)[:k]
+    rng = np.random.default_rng(seed)
+    rest = np.setdiff1d(np.arange(n), low)
+    return np.sort(np.concatenate([low, rng.choice(rest, k, replace=False)]))
+
+
+@pytest.mark.parametrize("n,k", [(262144, 256), (1048576, 64)])
+def test_centred_configuration_sizes(n, k):
+    # Acc and AccJerk of all N against all N (the automatic path at these
+    # sizes) checked on the lowest-|a| and random particles against the
+    # oracle, plus momentum balance sum_i m_i a_i = 0.
+    ps = ics.plummer(n, eps=1e-4, seed=2024)
+    assert lib.sweep_plan("acc_jerk_kernel", n, n)[0] == 1
+    idx = worst_and_random(ps, n, k, 1)
+    want_aj = oracle.run("acc_jerk_kernel", sub(ps, idx), ps)
+    got = run_centred("acc_jerk_kernel", ps, ps, policy=-1)
+    m = ps["m"]
+    for c in range(3):
+        assert abs(np.sum(m * got[c])) <= 1e-6 * np.sum(m * np.abs(got[c]))
+    gsub = tuple(g[idx] for g in got)
+    ea = vec_rel_err(gsub, want_aj, (0, 1, 2))
+    ej = vec_rel_err(gsub, want_aj, (3, 4, 5))
+    print("n=%d acc max %.3g median %.3g jerk max %.3g median %.3g" % (
+        n, ea.max(), np.median(ea), ej.max(), np.median(ej)))
+    assert ea.max() <= 1e-6, (ea.max(), np.median(ea))
+    assert np.median(ej) <= 1e-6 and ej.max() <= 1e-4, (ej.max(),
+                                                        np.median(ej))
+    want_a = oracle.run("acc_kernel", sub(ps, idx), ps)
+    got_a = run_centred("acc_kernel", ps, ps, policy=-1)
+    ea = vec_rel_err(tuple(g[idx] for g in got_a), want_a, (0, 1, 2))
+    assert ea.max() <= 1e-6, (ea.max(), np.median(ea))

@@ -29,14 +29,12 @@ def _configure(policy, gsplit):
     if policy == 1:
         lib.set_centred(1, -1, gsplit)
     else:
-        if hasattr(lib, "set_centred"):
-            lib.set_centred(0)
+        lib.set_centred(0)
         lib.set_split_config("acc_jerk_kernel", 9, gsplit)
 
 
 def _restore():
-    if hasattr(lib, "set_centred"):
-        lib.set_centred(-1, -1, 0)
+    lib.set_centred(-1, -1, 0)
     lib.set_split_config("acc_jerk_kernel", -1, 0)
 
 
@@ -59,7 +57,7 @@ def _sweep(torch, ps, n, policy, gsplit):
     return st, [o.cpu().numpy() for o in out]
 
 
-POLICIES = [(0, 1), (0, 4)]
+POLICIES = [(0, 1), (0, 4), (1, 1), (1, 4)]
 
 
 @pytest.mark.parametrize("policy,gsplit", POLICIES)

@@ -28,6 +28,7 @@ LIB32 = os.path.join(HERE, "libtupan_gb300_sp.so")
 UNITS = {
     "exact.o": ("exact.cu", ["-fmad=false"]),
     "split.o": ("split.cu", []),
+    "csweep.o": ("csweep.cu", []),
     "abi64.o": ("abi.cu", ["-DTG_ABI_FLOAT64"]),
     "abi32.o": ("abi.cu", ["-DTG_ABI_FLOAT32"]),
     "microbench.o": ("microbench.cu", []),
@@ -41,10 +42,10 @@ UNITS = {
     "nreg.o": ("nreg.cu", ["-fmad=false"]),
 }
 LINKS = {
-    LIB64: ["exact.o", "split.o", "abi64.o", "microbench.o", "driver.o",
+    LIB64: ["exact.o", "split.o", "csweep.o", "abi64.o", "microbench.o", "driver.o",
             "blockstep.o", "sakura.o", "mlp.o", "ensemble.o",
             "noalloc.o", "sia.o", "nreg.o"],
-    LIB32: ["exact.o", "split.o", "abi32.o", "microbench.o"],
+    LIB32: ["exact.o", "split.o", "csweep.o", "abi32.o", "microbench.o"],
 }
 
 

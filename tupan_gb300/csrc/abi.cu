@@ -59,6 +59,15 @@ bool split_supported(int kernel);
 bool split_has_x2(int kernel);
 bool split_has_raw(int kernel);
 int split_nf_host(int kernel);
+bool centred_supported(int k);
+int centred_shape_count();
+int centred_choose_gsplit(uint64_t ni, uint64_t nj, int shape, int sms);
+size_t centred_workspace_bytes(int k, uint64_t ni, uint64_t nj, bool same,
+                               int gsplit);
+cudaError_t launch_centred(int k, uint64_t ni, const void *const *ia,
+                           uint64_t nj, const void *const *ja, bool same,
+                           void *const *out, void *ws, int shape, int gsplit,
+                           unsigned *err, cudaStream_t st);
 }  // namespace tg
 
 namespace tg {
@@ -80,6 +89,15 @@ unsigned g_last_device_error = 0;
 int g_override_variant[K_COUNT];
 int g_override_gsplit[K_COUNT];
 bool g_override_init = false;
+// Centred sweeps: -1 automatic (large Phi/Acc/AccJerk sweeps), 0 never,
+// 1 always where supported; shape and grid split (< 0 / 0: automatic).
+int g_centred_policy = -1;
+int g_centred_shape = -1;
+int g_centred_gsplit = 0;
+// Sweeps of at least this many interactions (and 512 j) take the centred
+// path automatically: below it the sort and tile build cost more than the
+// sweep saves.
+constexpr double CENTRED_MIN_INTERACTIONS = 268435456.0;   // 2^28
 
 struct Tuned {
     int variant, gsplit;
@@ -251,6 +269,25 @@ void choose_split(const DeviceState *d, int kernel, uint64_t ni, uint64_t nj,
     }
 }
 
+// Whether a SPLIT sweep takes the centred kernels (csweep.cu).
+bool use_centred(int k, uint64_t ni, uint64_t nj)
+{
+    if (!centred_supported(k) || g_centred_policy == 0 || nj == 0) return false;
+    if (ni > 0xffffffffull || nj > 0xffffffffull) return false;
+    if (g_centred_policy == 1) return true;
+    return nj >= 512 && (double)ni * (double)nj >= CENTRED_MIN_INTERACTIONS;
+}
+
+// Launch shape and grid j-split of a centred sweep.
+void centred_plan(const DeviceState *d, uint64_t ni, uint64_t nj, int *shape,
+                  int *gsplit)
+{
+    *shape = g_centred_shape >= 0 ? g_centred_shape : 0;
+    *gsplit = g_centred_gsplit > 0
+                  ? g_centred_gsplit
+                  : centred_choose_gsplit(ni, nj, *shape, d->sms);
+}
+
 template <typename T>
 const T *cptr(const void *p) { return (const T *)p; }
 
@@ -276,6 +313,18 @@ int run_device_sweep(DeviceState *d, Sweep &s, cudaStream_t st)
             if (s.ip[a] != s.jp[a]) return false;
         return true;
     }();
+    if (use_centred(k, s.ni, s.nj)) {
+        int shape, gsplit;
+        centred_plan(d, s.ni, s.nj, &shape, &gsplit);
+        int rc = grow(&d->pack, &d->pack_bytes,
+                      centred_workspace_bytes(k, s.ni, s.nj, same, gsplit),
+                      "centred sweep workspace");
+        if (rc) return rc;
+        e = launch_centred(k, s.ni, s.ip, s.nj, s.jp, same, s.out, d->pack,
+                           shape, gsplit, d->err, st);
+        if (e != cudaSuccess) return cuda_fail(e, "centred sweep launch");
+        return ST_OK;
+    }
     int variant, gsplit;
     choose_split(d, k, s.ni, s.nj, &variant, &gsplit);
     const size_t ibytes = (size_t)s.ni * nf * sizeof(float4);
@@ -760,6 +809,43 @@ TG_EXPORT int tupan_gb300_split_choice(int kernel, uint64_t ni, uint64_t nj,
     int rc = device_state(&d);
     if (rc) return rc;
     choose_split(d, kernel, ni, nj, variant, gsplit);
+    return ST_OK;
+}
+
+// Centred SPLIT sweeps (Phi, Acc, AccJerk on Morton-ordered, tile-centred
+// records; csweep.cu): policy -1 automatic (sweeps of at least 2^28
+// interactions), 0 never, 1 always; shape < 0 and gsplit <= 0 automatic.
+// Returns ST_OK or ST_BAD_ARGUMENT.
+TG_EXPORT int tupan_gb300_set_centred(int policy, int shape, int gsplit)
+{
+    std::lock_guard<std::mutex> lock(g_mu);
+    if (policy < -1 || policy > 1 || shape >= centred_shape_count())
+        return ST_BAD_ARGUMENT;
+    g_centred_policy = policy;
+    g_centred_shape = shape;
+    g_centred_gsplit = gsplit;
+    return ST_OK;
+}
+
+// The path a SPLIT sweep of this size takes: *path 1 (centred, *config =
+// launch shape) or 0 (split variants, *config = variant); *gsplit the grid
+// j-split.
+TG_EXPORT int tupan_gb300_sweep_plan(int kernel, uint64_t ni, uint64_t nj,
+                                     int *path, int *config, int *gsplit)
+{
+    std::lock_guard<std::mutex> lock(g_mu);
+    init_overrides();
+    if (kernel < 0 || kernel >= K_COUNT) return ST_BAD_ARGUMENT;
+    DeviceState *d;
+    int rc = device_state(&d);
+    if (rc) return rc;
+    if (use_centred(kernel, ni, nj)) {
+        *path = 1;
+        centred_plan(d, ni, nj, config, gsplit);
+    } else {
+        *path = 0;
+        choose_split(d, kernel, ni, nj, config, gsplit);
+    }
     return ST_OK;
 }
 

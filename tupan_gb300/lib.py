@@ -69,6 +69,11 @@ def _declare(L):
     L.tupan_gb300_kernel_arity.restype = c.c_int
     L.tupan_gb300_device_sms.restype = c.c_int
     L.tupan_gb300_real_bits.restype = c.c_int
+    L.tupan_gb300_set_centred.argtypes = [c.c_int, c.c_int, c.c_int]
+    L.tupan_gb300_set_centred.restype = c.c_int
+    L.tupan_gb300_sweep_plan.argtypes = [c.c_int, c.c_uint64, c.c_uint64] + [
+        c.POINTER(c.c_int)] * 3
+    L.tupan_gb300_sweep_plan.restype = c.c_int
     L.tupan_gb300_set_pipe_spin_limit.argtypes = [c.c_uint]
     L.tupan_gb300_set_pipe_spin_limit.restype = c.c_uint
 
@@ -134,6 +139,28 @@ def split_variants():
         out.append({"ni_per_thread": a.value, "jsplit": b.value,
                     "threads": c.value})
     return out
+
+
+def set_centred(policy=-1, shape=-1, gsplit=0, prec="float64"):
+    """Centred SPLIT sweeps (Phi/Acc/AccJerk): policy -1 automatic, 0 never,
+    1 always; shape below 0 / gsplit at most 0: automatic."""
+    st = load(prec).tupan_gb300_set_centred(int(policy), int(shape),
+                                            int(gsplit))
+    if st:
+        raise TupanGB300Error("bad centred config")
+
+
+def sweep_plan(kernel, ni, nj):
+    """(path, config, gsplit) of a SPLIT sweep: path 1 = centred (config =
+    launch shape), 0 = split variants (config = variant)."""
+    L = load("float64")
+    p, c, g = ctypes.c_int(), ctypes.c_int(), ctypes.c_int()
+    st = L.tupan_gb300_sweep_plan(KERNEL_ID[kernel], int(ni), int(nj),
+                                  ctypes.byref(p), ctypes.byref(c),
+                                  ctypes.byref(g))
+    if st:
+        check()
+    return p.value, c.value, g.value
 
 
 def set_pipe_spin_limit(limit, prec="float64"):
