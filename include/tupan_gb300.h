@@ -264,18 +264,22 @@ long long tupan_gb300_hermite_tau_log(void *handle, double *out,
 int tupan_gb300_hermite_energy(void *handle, double *ke, double *pe);
 int tupan_gb300_hermite_destroy(void *handle);
 
-/* No counterpart in the reference.  acc_jerk_kernel's arithmetic in SPLIT
- * mode on DEVICE arrays (argument order of libtupan.h:34-58, then a stream
- * and an optional host pointer for the error word), for callers that cannot
- * let the library allocate device memory: an application whose memory
- * manager owns the whole device heap, or a step loop that must not stall on
- * cudaMalloc's device-wide synchronisation.  Its scratch (packed particle
- * records) is a static device array of 6 MiB, so ni and nj are limited to
- * 65536 each; larger requests return 5 before anything runs.  All calls
- * share that array: calls that overlap on the GPU race.  The first call on a
- * device looks up the array's address there; make it outside stream capture.
- * err_out == NULL: asynchronous; otherwise the call waits for the stream and
- * stores the sweep's device error word.  Returns 0 or a status code. */
+/* No counterpart in the reference.  The acc_jerk sum in SPLIT arithmetic on
+ * DEVICE arrays, for callers that cannot let the library allocate device
+ * memory: an application whose memory manager owns the whole device heap,
+ * or a step loop that must not stall on cudaMalloc's device-wide
+ * synchronisation.  Arguments: ni and the i-set's m, rx, ry, rz, e2, vx, vy,
+ * vz; nj and the j-set's eight arrays in the same order; the outputs ax, ay,
+ * az, jx, jy, jz (ni each); a cudaStream_t (NULL: the default stream); an
+ * optional host pointer for the device error word.  Its scratch (packed
+ * particle records and grid j-split partial sums) is 12 MiB of static device
+ * arrays, so ni and nj are limited to 65536 each; larger requests return 5
+ * before anything runs.  All calls share those arrays: calls that overlap on
+ * the GPU race.  The first call on a device looks up the arrays' addresses
+ * there; make it outside stream capture.  err_out == NULL: asynchronous, and
+ * no device error is reported; otherwise the call waits for the stream,
+ * stores the sweep's device error word and returns 3 if it is non-zero.
+ * Returns 0 or a status code. */
 int tupan_gb300_acc_jerk_split_noalloc(
     uint64_t ni, const double *im, const double *irx, const double *iry,
     const double *irz, const double *ie2, const double *ivx,
