@@ -247,6 +247,41 @@ def kepler_solves(torch, stream):
     return res
 
 
+def noalloc_rate(torch, dev, ps, stream):
+    """The allocation-free acc_jerk entry at its largest size (65536 i
+    against 65536 j of the sphere's first particles), interactions/s."""
+    import ctypes
+    from tupan_gb300 import lib
+    L = lib.load()
+    f = L.tupan_gb300_acc_jerk_split_noalloc
+    f.argtypes = ([ctypes.c_uint64] + [ctypes.c_void_p] * 8
+                  + [ctypes.c_uint64] + [ctypes.c_void_p] * 8
+                  + [ctypes.c_void_p] * 6 + [ctypes.c_void_p,
+                                             ctypes.POINTER(ctypes.c_uint)])
+    f.restype = ctypes.c_int
+    n = min(65536, len(ps["m"]))
+    names = ("m", "rx", "ry", "rz", "e2", "vx", "vy", "vz")
+    d = [torch.from_numpy(np.ascontiguousarray(ps[k][:n])).to(dev)
+         for k in names]
+    o = [torch.empty(n, dtype=torch.float64, device=dev) for _ in range(6)]
+    args = ([n] + [x.data_ptr() for x in d] + [n] + [x.data_ptr() for x in d]
+            + [x.data_ptr() for x in o] + [stream, None])
+    f(*args)
+    torch.cuda.synchronize()
+    ts = []
+    for _ in range(3):
+        a = torch.cuda.Event(enable_timing=True)
+        b = torch.cuda.Event(enable_timing=True)
+        a.record()
+        st = f(*args)
+        b.record()
+        torch.cuda.synchronize()
+        if st:
+            return None
+        ts.append(a.elapsed_time(b) / 1e3)
+    return {"n": n, "gints": n * n / min(ts) / 1e9}
+
+
 def reference_step(ps, sub):
     """One Acc + AccJerk sweep of the i-subset `sub` against all of `ps` on
     the host: the reference kernels compiled from their own sources
@@ -387,28 +422,21 @@ def main():
     inter = 2.0 * n * n
     value = job_rate(inter, world, t_step)
 
-    # --- end to end through the reference-facing C-ABI (host arrays), right
-    # after the device-timed steps so both see the same clocks ------------
-    pinned = {k: torch.from_numpy(ps[k]).pin_memory() for k in names8}
-    hp = {k: pinned[k].numpy() for k in names8}
-    h_acc = [torch.empty(n, dtype=torch.float64).pin_memory().numpy()
-             for _ in range(3)]
-    h_aj = [torch.empty(n, dtype=torch.float64).pin_memory().numpy()
-            for _ in range(6)]
-    from tupan_gb300 import abi
-    f_acc = lib.bind("acc_kernel")
-    f_aj = lib.bind("acc_jerk_kernel")
+    # --- end to end through the drop-in plugin object (tupan's extension
+    # surface: Acc / AccJerk .calc -> CUDAKernel.run -> acc_kernel /
+    # acc_jerk_kernel C-ABI) on ordinary pageable numpy arrays, as tupan's
+    # ParticleSystem holds them; right after the device-timed steps so both
+    # see the same clocks --------------------------------------------------
+    from tupan_gb300 import extensions
+    from tupan_gb300.particles import Bodies
+    bodies = Bodies(ps)
+    x_acc = extensions.Acc("CUDA", "float64")
+    x_aj = extensions.AccJerk("CUDA", "float64")
     old_mode = lib.set_mode(lib.MODE_SPLIT)
 
     def host_step():
-        va = abi.make_args("acc_kernel", "float64", hp, hp, None,
-                           {"iax": h_acc[0], "iay": h_acc[1], "iaz": h_acc[2]})
-        abi.call(f_acc, "acc_kernel", "float64", va)
-        vj = abi.make_args("acc_jerk_kernel", "float64", hp, hp, None,
-                           dict(zip(("iax", "iay", "iaz", "ijx", "ijy", "ijz"),
-                                    h_aj)))
-        abi.call(f_aj, "acc_jerk_kernel", "float64", vj)
-        lib.check()
+        x_acc.calc(bodies, bodies)
+        x_aj.calc(bodies, bodies)
 
     host_step()
     e2e_clocks = ClockSampler(local)
@@ -457,6 +485,7 @@ def main():
     if rank == 0 and v_nr is not None:
         for name in ("acc_kernel", "acc_jerk_kernel"):
             lib.set_split_config(name, v_nr, g_def)
+        lib.set_centred(0)
         try:
             step()
             f0, f1, f2 = (torch.cuda.Event(enable_timing=True)
@@ -475,6 +504,7 @@ def main():
         finally:
             for name in ("acc_kernel", "acc_jerk_kernel"):
                 lib.set_split_config(name, -1, 0)
+            lib.set_centred(-1, -1, 0)
         got = [t.cpu().numpy()[idx] for t in d_aj]
         rel = (np.linalg.norm(np.stack(got[:3]) - wa, axis=0) /
                np.linalg.norm(wa, axis=0))
@@ -485,6 +515,34 @@ def main():
                   "acc_rel_err_vs_fp64": {
                       "max": float(rel.max()),
                       "median": float(np.median(rel))}}
+
+    # --- the same sweeps on the double-single split variants (the path
+    # the centred kernels replace at this size), for comparison ------------
+    variants_cmp = None
+    if rank == 0:
+        lib.set_centred(0)
+        try:
+            step()
+            f0, f1, f2 = (torch.cuda.Event(enable_timing=True)
+                          for _ in range(3))
+            flush.fill_(0.25)
+            f0.record(stream)
+            lib.dev_sweep("acc_kernel", n, p5, n, p5,
+                          [t.data_ptr() for t in d_acc], mode=lib.MODE_SPLIT,
+                          stream=sh)
+            f1.record(stream)
+            lib.dev_sweep("acc_jerk_kernel", n, p8, n, p8,
+                          [t.data_ptr() for t in d_aj], mode=lib.MODE_SPLIT,
+                          stream=sh)
+            f2.record(stream)
+            torch.cuda.synchronize()
+            v_sv, g_sv = lib.split_choice("acc_jerk_kernel", n, n)
+        finally:
+            lib.set_centred(-1, -1, 0)
+        variants_cmp = {
+            "variant": v_sv, "gsplit": g_sv,
+            "acc_split_gints": n * n / (f0.elapsed_time(f1) / 1e3) / 1e9,
+            "acc_jerk_split_gints": n * n / (f1.elapsed_time(f2) / 1e3) / 1e9}
 
     # --- FP64 EXACT path on an i-subset (linear in ni) ---------------------
     ni64 = min(args.fp64_ni, n)
@@ -526,6 +584,7 @@ def main():
 
 
     kepler = kepler_solves(torch, stream) if rank == 0 else None
+    noalloc = noalloc_rate(torch, dev, ps, sh) if rank == 0 else None
 
     if rank != 0:
         if world > 1:
@@ -534,7 +593,10 @@ def main():
     cpu = None if args.no_cpu else cpu_baseline(n, args.cpu_ni, ps)
     achieved = n * n * FLOPS_ACC_JERK / t_aj / 1e12
     traffic = roofline_traffic()
-    v_aj, g_aj = lib.split_choice("acc_jerk_kernel", n, n)
+    path_aj, cfg_aj, g_aj = lib.sweep_plan("acc_jerk_kernel", n, n)
+    kname = ("ct_sweep<CtAccJerk> (centred, shape %d)" % cfg_aj
+             if path_aj == 1 else
+             "split_sweep<AccJerkS> variant %d" % cfg_aj)
     line = {
         "metric": METRIC, "value": value, "unit": "Gint/s",
         "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
@@ -546,7 +608,8 @@ def main():
                    "n": n, "interactions_per_step": inter,
                    "l2": "flushed between steps (256 MiB write)",
                    "parallelism": "replicas" if world > 1 else "single GPU",
-                   "acc_jerk_variant": v_aj, "acc_jerk_gsplit": g_aj},
+                   "acc_jerk_path": "centred" if path_aj == 1 else "split",
+                   "acc_jerk_config": cfg_aj, "acc_jerk_gsplit": g_aj},
         "kernels": {"acc_split_gints": n * n / t_acc / 1e9,
                     "acc_jerk_split_gints": n * n / t_aj / 1e9,
                     "fp64_exact_gints": fp64_gints,
@@ -554,9 +617,11 @@ def main():
                     "fp64_sample_ni": ni64,
                     "split_over_fp64": (inter / t_step) / (2.0 * ni64 * n / t64),
                     "acc_rel_err_vs_fp64": acc_err,
-                    "newton_form": newton},
+                    "newton_form": newton,
+                    "split_variants_path": variants_cmp,
+                    "noalloc_acc_jerk": noalloc},
         "roofline": {"bound": "fp32",
-                     "kernel": "split_sweep<AccJerkS> variant %d" % v_aj,
+                     "kernel": kname,
                      "achieved": achieved, "peak": fp32_peak,
                      "unit": "TFLOP/s", "frac": achieved / fp32_peak,
                      "flops_per_interaction": FLOPS_ACC_JERK,
@@ -568,9 +633,10 @@ def main():
         "cpu_baseline": cpu,
         "e2e": {"value": e2e_val, "unit": "Gint/s",
                 "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
-                "path": "acc_kernel + acc_jerk_kernel C-ABI, pinned host "
-                        "arrays, SPLIT mode", "ms_per_step": t_e2e * 1e3,
-                "clocks": e2e_clk},
+                "path": "tupan_gb300.extensions Acc/AccJerk .calc(ps, ps) -> "
+                        "CUDAKernel.run -> acc_kernel / acc_jerk_kernel C-ABI, "
+                        "pageable numpy arrays, SPLIT mode",
+                "ms_per_step": t_e2e * 1e3, "clocks": e2e_clk},
         "kepler": kepler,
         "gpu_launches": int(launches),
         "clocks": clk,
