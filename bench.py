@@ -221,20 +221,42 @@ def kepler_solves(torch, stream):
         return min(ts)
 
     res = {"pairs": n, "dt": dt}
-    t = best(lambda: kp.kepler_pairs(n, dt, sm, se, ss, out, iters=it))
-    res["solves_per_s_plain"] = n / t
-    res["mean_iters_plain"] = float(it.float().mean().item())
+    # the three root-solve forms (reference structure; one cos/sin per
+    # Laguerre update, bit-identical; FP32 then FP64 updates), plain start
+    for form in ("reference", "shared", "mixed"):
+        old_form = kp.set_form(form)
+        try:
+            t = best(lambda: kp.kepler_pairs(n, dt, sm, se, ss, out,
+                                             iters=it))
+        finally:
+            kp.set_form(old_form)
+        res["solves_per_s_%s" % form] = n / t
+        res["mean_fp64_updates_%s" % form] = float(it.float().mean().item())
+    res["solves_per_s_plain"] = res["solves_per_s_reference"]
+    res["mean_iters_plain"] = res["mean_fp64_updates_reference"]
     try:
         net = learned.LearnedStart.load()
         net.install()
-        t = best(lambda: kp.kepler_pairs(n, dt, sm, se, ss, out, iters=it,
-                                         use_mlp=True))
-        res["solves_per_s_learned"] = n / t
-        res["mean_iters_learned"] = float(it.float().mean().item())
+        for form in ("reference", "mixed"):
+            old_form = kp.set_form(form)
+            try:
+                t = best(lambda: kp.kepler_pairs(n, dt, sm, se, ss, out,
+                                                 iters=it, use_mlp=True))
+            finally:
+                kp.set_form(old_form)
+            res["solves_per_s_learned_%s" % form] = n / t
+            res["mean_fp64_updates_learned_%s" % form] = float(
+                it.float().mean().item())
+        res["solves_per_s_learned"] = res["solves_per_s_learned_reference"]
         res["learned_gate"] = net.gate
         kp.clear_mlp()
     except (OSError, KeyError):
         res["solves_per_s_learned"] = None
+    if res.get("solves_per_s_learned_mixed"):
+        res["learned_mixed_over_plain_reference"] = (
+            res["solves_per_s_learned_mixed"] / res["solves_per_s_reference"])
+        res["learned_mixed_over_plain_shared"] = (
+            res["solves_per_s_learned_mixed"] / res["solves_per_s_shared"])
     ps = ics.plummer(4096, eps=0.0, seed=11, masses="salpeter")
     names = ("m", "rx", "ry", "rz", "e2", "vx", "vy", "vz")
     d = {k: T(ps[k]) for k in names}
@@ -244,6 +266,12 @@ def kepler_solves(torch, stream):
     op = [x.data_ptr() for x in o]
     t = best(lambda: kp.sakura_queue(4096, p, 4096, p, op, dt, -1))
     res["sakura_pairs_per_s"] = 4096 * 4096 / t
+    old_form = kp.set_form("mixed")
+    try:
+        t = best(lambda: kp.sakura_queue(4096, p, 4096, p, op, dt, -1))
+    finally:
+        kp.set_form(old_form)
+    res["sakura_pairs_per_s_mixed"] = 4096 * 4096 / t
     return res
 
 

@@ -336,6 +336,15 @@ int tupan_gb300_kepler_set_mlp(const void *w1, const float *b1,
                                const void *w2, const float *b2,
                                const void *w3, const float *b3,
                                const float *norm, float gate);
+/* Form of the universal-Kepler root solve for kepler_pairs, sakura_queue and
+ * the device Sakura integrator (no counterpart in the reference): 0 the
+ * reference's structure (default), 1 the same arithmetic with cos/sin (or
+ * cosh/sinh) evaluated once per Laguerre update (bit-identical results),
+ * 2 mixed precision: FP32 Laguerre updates, then FP64 updates until the
+ * reference's 2^-42 tolerance is met.  The libtupan.h entry points always use
+ * form 0.  Returns the previous form, or -1 for an unknown form. */
+int tupan_gb300_kepler_set_form(int form);
+
 /* n independent pairs over dt: m[n], e2[n], state[n x 6] (relative r, v)
  * -> out[n x 6].  iters[n] (Laguerre updates), rec_x[n x 4] and rec_y[n]
  * (learned-start features and targets) may be NULL.  Synchronous. */

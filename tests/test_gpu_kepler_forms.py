@@ -1,0 +1,135 @@
+"""Forms of the universal-Kepler root solve (tg_kepler.cuh).
+
+* "shared" evaluates cos/sin (cosh/sinh) once per Laguerre update instead of
+  once per Stumpff function: the same operations on the same values, so the
+  results must be bit-identical to the reference form.
+* "mixed" iterates in FP32, then takes FP64 Laguerre updates until the
+  reference's 2^-42 tolerance is met (or predicted to be met by the next
+  update).  Its final states must agree with the oracle's full solve (the
+  reference's arithmetic) within the bound the reference form is held to,
+  1e-12 of the coordinate scale, with fewer FP64 updates.
+"""
+
+import numpy as np
+import pytest
+
+import oracle
+from tupan_gb300 import ics, learned
+from tupan_gb300 import kepler as kp
+
+pytestmark = pytest.mark.gpu
+NAMES = ("m", "rx", "ry", "rz", "e2", "vx", "vy", "vz")
+
+
+def pair_set(n, seed, soft=False):
+    rng = np.random.default_rng(seed)
+    m = rng.uniform(1e-4, 1e-2, n)
+    e2 = rng.uniform(1e-9, 1e-8, n) if soft else np.zeros(n)
+    r = rng.uniform(1e-3, 5e-2, n)
+    u = rng.standard_normal((n, 3))
+    u /= np.linalg.norm(u, axis=1, keepdims=True)
+    w = rng.standard_normal((n, 3))
+    vc = np.sqrt(m / r)[:, None]
+    # bound (0.2-1.2 x circular) and unbound (up to 2 x) pairs
+    st = np.concatenate([u * r[:, None],
+                         w * vc * rng.uniform(0.2, 2.0, (n, 1))], axis=1)
+    return m, e2, st
+
+
+def solve(torch, form, dt, m, e2, st, use_mlp=False):
+    T = lambda a: torch.from_numpy(np.ascontiguousarray(a)).cuda()
+    n = len(m)
+    out = torch.zeros((n, 6), dtype=torch.float64, device="cuda")
+    iters = torch.zeros(n, dtype=torch.int32, device="cuda")
+    old = kp.set_form(form)
+    try:
+        kp.kepler_pairs(n, dt, T(m), T(e2), T(st), out, iters=iters,
+                        use_mlp=use_mlp)
+    finally:
+        kp.set_form(old)
+    return out.cpu().numpy(), iters.cpu().numpy()
+
+
+# Softened pairs only at the short step: over long steps the reference's
+# energy check keeps subdividing softened eccentric orbits until the solve
+# budget runs out, which is slow in both the library and the oracle.
+CASES = [(1.0 / 512, False), (1.0 / 32, False), (1.0 / 4, False),
+         (1.0 / 512, True)]
+
+
+@pytest.mark.parametrize("dt,soft", CASES)
+def test_shared_form_bit_identical(dt, soft):
+    torch = pytest.importorskip("torch")
+    m, e2, st = pair_set(3000, 7, soft)
+    a, ia = solve(torch, "reference", dt, m, e2, st)
+    b, ib = solve(torch, "shared", dt, m, e2, st)
+    np.testing.assert_array_equal(a, b)
+    np.testing.assert_array_equal(ia, ib)
+
+
+@pytest.mark.parametrize("dt,soft", CASES)
+def test_mixed_form_matches_oracle(dt, soft):
+    torch = pytest.importorskip("torch")
+    m, e2, st = pair_set(3000, 8, soft)
+    want, it_w, _ = oracle.kepler_pairs(dt, m, e2, st)
+    got, it_g = solve(torch, "mixed", dt, m, e2, st)
+    scale = np.abs(st).max(axis=1, keepdims=True)
+    assert np.all(np.abs(got - want) <= 1e-12 * scale)
+    # FP64 updates: the reference form needs at least two per solve (one to
+    # move, one to see the update fall below the tolerance)
+    assert it_g.mean() < it_w.mean()
+
+
+def test_mixed_form_on_sakura_pairs_with_learned_start():
+    torch = pytest.importorskip("torch")
+    dt = 1.0 / 512
+    st, m, e2 = learned.kepler_pair_states(2048, 11, dt, flag=-1)
+    want, _ = solve(torch, "reference", dt, m, e2, st)
+    got, it = solve(torch, "mixed", dt, m, e2, st)
+    scale = np.abs(st).max(axis=1, keepdims=True)
+    assert np.all(np.abs(got - want) <= 1e-12 * scale)
+    assert it.mean() <= 1.05
+    try:
+        net = learned.LearnedStart.load()
+    except (OSError, KeyError):
+        pytest.skip("no trained start network shipped")
+    net.install()
+    try:
+        got2, _ = solve(torch, "mixed", dt, m, e2, st, use_mlp=True)
+    finally:
+        kp.clear_mlp()
+    assert np.all(np.abs(got2 - want) <= 1e-12 * scale)
+
+
+@pytest.mark.parametrize("flag", [-1, 1])
+def test_sakura_queue_mixed_form_matches_oracle(flag):
+    torch = pytest.importorskip("torch")
+    ps = ics.plummer(1024, eps=0.0, seed=5, masses="salpeter")
+    d = {k: torch.from_numpy(np.ascontiguousarray(ps[k])).cuda()
+         for k in NAMES}
+    out = [torch.zeros(1024, dtype=torch.float64, device="cuda")
+           for _ in range(6)]
+    dt = 1.0 / 512
+    old = kp.set_form("mixed")
+    try:
+        nk, _ = kp.sakura_queue(1024, [d[k].data_ptr() for k in NAMES], 1024,
+                                [d[k].data_ptr() for k in NAMES],
+                                [o.data_ptr() for o in out], dt, flag)
+    finally:
+        kp.set_form(old)
+    assert nk > 0
+    want = oracle.run("sakura_kernel", ps, ps, {"dt": dt, "flag": flag})
+    rs = max(np.abs(ps[k]).max() for k in ("rx", "ry", "rz"))
+    vs = max(np.abs(ps[k]).max() for k in ("vx", "vy", "vz"))
+    for c in range(6):
+        g = out[c].cpu().numpy()
+        atol = 1e-12 * (rs if c < 3 else vs)
+        assert np.max(np.abs(g - want[c])) <= atol, c
+
+
+def test_set_form_rejects_unknown():
+    pytest.importorskip("torch")
+    with pytest.raises(KeyError):
+        kp.set_form("quad")
+    L = kp._lib()
+    assert L.tupan_gb300_kepler_set_form(7) == -1

@@ -155,6 +155,7 @@ struct PairSolve {
     float *rec_x, *rec_y;           // n x 4 features, n targets (or null)
     long long budget;
     int use_mlp;
+    int form;                       // KeplerForm of the single-step solves
     MlpParams mlp;
 };
 
@@ -170,6 +171,7 @@ k_pair_solve(const PairSolve P, unsigned *err)
     for (int c = 0; c < 6; ++c) p0[c] = P.state[6 * q + c];
     const double m = P.m[q], e2 = P.e2[q];
     KepCtx<double> ctx = {0, P.budget, 0, false, false, 0.0};
+    ctx.form = P.form;
     KepArg<double> ka;
     double s0;
     const bool moving = kep_setup(P.dt, m, e2, p0, &ka, &s0);
@@ -215,6 +217,7 @@ struct SakuraArgs {
     int *iters;             // per queued pair (or null)
     long long budget;
     int use_mlp;
+    int form;               // KeplerForm of the Kepler-branch solves
     MlpParams mlp;
 };
 
@@ -426,6 +429,7 @@ k_sakura_kepler(const SakuraArgs A, uint64_t nq, unsigned *err)
     double p0[6], pre[6], m, e2, p1[6];
     sk_kepler(ip, jp, A.dt, A.flag, p0, pre, &m, &e2);
     KepCtx<double> ctx = {0, A.budget, 0, false, false, 0.0};
+    ctx.form = A.form;
     if (A.use_mlp) {
         KepArg<double> ka;
         double s0;
@@ -484,6 +488,7 @@ struct SakuraWork {
 SakuraWork g_work;
 MlpParams g_mlp;
 bool g_have_mlp = false;
+int g_kepler_form = KEP_REFERENCE;   // tupan_gb300_kepler_set_form
 
 int grow_queue(size_t nq)
 {
@@ -536,6 +541,21 @@ TG_EXPORT int tupan_gb300_kepler_set_mlp(const void *w1, const float *b1,
     return ST_OK;
 }
 
+// Form of the universal-Kepler root solve used by the pair solver, the
+// queued Sakura sweep and the device Sakura integrator: 0 the reference's
+// structure (default), 1 the same arithmetic with one cos/sin (cosh/sinh)
+// per Laguerre update (bit-identical), 2 FP32 Laguerre updates then FP64
+// updates to the reference's 2^-42 tolerance (see tg_kepler.cuh).  The ten
+// libtupan.h entry points always use form 0.  Returns the previous form, or
+// -1 for an unknown one.
+TG_EXPORT int tupan_gb300_kepler_set_form(int form)
+{
+    if (form < KEP_REFERENCE || form > KEP_MIXED) return -1;
+    const int old = g_kepler_form;
+    g_kepler_form = form;
+    return old;
+}
+
 // Solves n independent pairs (DEVICE arrays: m, e2, state n x 6, out n x 6)
 // over dt with universal_kepler_solver's full retry logic; iters, rec_x
 // (n x 4) and rec_y (n) are optional.  use_mlp selects the learned start.
@@ -565,6 +585,7 @@ TG_EXPORT int tupan_gb300_kepler_pairs(uint64_t n, double dt, const double *m,
     P.rec_y = rec_y;
     P.budget = budget > 0 ? budget : (1LL << 20);
     P.use_mlp = use_mlp;
+    P.form = g_kepler_form;
     P.mlp = g_mlp;
     if (n) {
         k_pair_solve<<<(unsigned)((n + 127) / 128), 128, 0, st>>>(P, g_work.err);
@@ -624,6 +645,7 @@ TG_EXPORT int tupan_gb300_sakura_queue(uint64_t ni, const void *const *i_attrs,
     A.cnt = g_work.cnt;
     A.budget = budget > 0 ? budget : (1LL << 20);
     A.use_mlp = use_mlp;
+    A.form = g_kepler_form;
     A.mlp = g_mlp;
     cudaMemsetAsync(g_work.err, 0, sizeof(unsigned), st);
     const unsigned blocks = (unsigned)((ni + SK_THREADS - 1) / SK_THREADS);

@@ -122,6 +122,29 @@ __device__ int kep_laguerre(R x0, R *x, const KepArg<R> &k, int *iters)
     return 0;
 }
 
+// set_new_pos_vel, universal_kepler_solver.h:312-357, from S1..S3 at the root
+template <typename R>
+__device__ void kep_update_S(R dt, const R *S, R r0, R m, R e2, R *p)
+{
+    R r0x = p[0], r0y = p[1], r0z = p[2];
+    R v0x = p[3], v0y = p[4], v0z = p[5];
+    R lf = R(1) - m * S[2] / r0;
+    R lg = dt - m * S[3];
+    R r1x = r0x * lf + v0x * lg;
+    R r1y = r0y * lf + v0y * lg;
+    R r1z = r0z * lf + v0z * lg;
+    R r1sq = r1x * r1x + r1y * r1y + r1z * r1z;
+    R r1 = sqrt(r1sq + e2);
+    R ldf = -m * S[1] / (r0 * r1);
+    R ldg = (R(1) + lg * ldf) / lf;
+    p[0] = r1x;
+    p[1] = r1y;
+    p[2] = r1z;
+    p[3] = r0x * ldf + v0x * ldg;
+    p[4] = r0y * ldf + v0y * ldg;
+    p[5] = r0z * ldf + v0z * ldg;
+}
+
 // set_new_pos_vel, universal_kepler_solver.h:312-357
 template <typename R>
 __device__ void kep_update(R dt, R s, R r0, R m, R e2, R al, R *p)
@@ -145,16 +168,258 @@ __device__ void kep_update(R dt, R s, R r0, R m, R e2, R al, R *p)
     p[5] = r0z * ldf + v0z * ldg;
 }
 
+// ---------------------------------------------------------------------------
+// Forms of the single-step root solve.
+//   KEP_REFERENCE  the reference's structure: each of S0..S3 evaluates its own
+//                  sqrt and cos/sin (or cosh/sinh), six per Laguerre update.
+//   KEP_SHARED     the same arithmetic with cos/sin (cosh/sinh) of the one
+//                  argument of an update evaluated once: bit-identical roots
+//                  and states, a sixth of the transcendentals.
+//   KEP_MIXED      Laguerre updates in FP32 (Stumpff c2, c3 from their power
+//                  series where the closed forms cancel), then FP64 Laguerre
+//                  updates until the predicted next update is below the
+//                  reference's tolerance, and S1..S3 at the root by a Taylor
+//                  shift from the last FP64 evaluation: about one FP64
+//                  cos/sin per solve.
+// ---------------------------------------------------------------------------
+enum KeplerForm : int { KEP_REFERENCE = 0, KEP_SHARED = 1, KEP_MIXED = 2 };
+
 // Per-solve bookkeeping: budget, counters and the optional learned start.
 template <typename R>
 struct KepCtx {
     long long solves;      // single-step solves spent on this pair solve
     long long budget;      // upper bound on `solves`
-    long long iterations;  // Laguerre updates summed
+    long long iterations;  // Laguerre updates summed (FP64 updates, KEP_MIXED)
     bool exhausted;
     bool use_start;        // take `start` instead of dt/r on the first try
     R start;
+    int form = KEP_REFERENCE;
+    long long iterations32 = 0;   // FP32 updates (KEP_MIXED)
 };
+
+// Stumpff c0..c3 of z from one transcendental evaluation: the reference's
+// closed forms (universal_kepler_solver.h:17-79) with cos(w), sin(w) (or
+// cosh, sinh) of w = sqrt(|z|) computed once; each value is the one the
+// separate functions return.
+template <typename R>
+__device__ __forceinline__ void stumpff_all(R z, R *c)
+{
+    if (z < R(0)) {
+        const R w = sqrt(-z);
+        const R cw = cos(w), sw = sin(w);
+        const R s1 = sw / w;
+        c[0] = cw;
+        c[1] = s1;
+        c[2] = (cw - R(1)) / z;
+        c[3] = (s1 - R(1)) / z;
+    } else if (z > R(0)) {
+        const R w = sqrt(z);
+        const R cw = cosh(w), sw = sinh(w);
+        const R s1 = sw / w;
+        c[0] = cw;
+        c[1] = s1;
+        c[2] = (cw - R(1)) / z;
+        c[3] = (s1 - R(1)) / z;
+    } else {
+        c[0] = R(1);
+        c[1] = R(1);
+        c[2] = R(1) / R(2);
+        c[3] = R(1) / R(6);
+    }
+}
+
+// S0..S3 at s (the products of kS0..kS3, universal_kepler_solver.h:82-120).
+template <typename R>
+__device__ __forceinline__ void kep_S(R s, R al, R *S)
+{
+    R c[4];
+    const R s2 = s * s;
+    stumpff_all(al * s2, c);
+    S[0] = c[0];
+    S[1] = s * c[1];
+    S[2] = s2 * c[2];
+    S[3] = (s * s2) * c[3];
+}
+
+// f, f', f'' of universal_kepler{,_ds,_dsds} from precomputed S values.
+template <typename R>
+__device__ __forceinline__ void kep_fdd(const R *S, R s, const KepArg<R> &k,
+                                        R *f, R *df, R *ddf)
+{
+    const R b = k.m + k.al * k.r0;
+    *f = (k.r0 * s + k.rv0 * S[2] + b * S[3]) - k.dt;
+    *df = k.r0 + k.rv0 * S[1] + b * S[2];
+    *ddf = k.rv0 * S[0] + b * S[1];
+}
+
+// One Laguerre update of order 5 (universal_kepler_solver.h:233-243);
+// false when the denominator vanishes.
+template <typename R>
+__device__ __forceinline__ bool lag_delta(R fv, R dfv, R ddfv, R *delta)
+{
+    const int ORDER = 5;
+    const R a = dfv;
+    const R a2 = a * a;
+    const R b = a2 - fv * ddfv;
+    const R g = R(ORDER) * fv;
+    const R h = a + R(sgn(a)) * sqrt(fabs(R(ORDER - 1) * (R(ORDER) * b - a2)));
+    if (h == R(0)) return false;
+    *delta = -g / h;
+    return true;
+}
+
+// kep_laguerre with one S evaluation per update (KEP_SHARED).
+template <typename R>
+__device__ int kep_laguerre_shared(R x0, R *x, const KepArg<R> &k, int *iters)
+{
+    int it = 0;
+    R delta;
+    *x = x0;
+    do {
+        R S[4], fv, dfv, ddfv;
+        kep_S(*x, k.al, S);
+        kep_fdd(S, *x, k, &fv, &dfv, &ddfv);
+        if (!lag_delta(fv, dfv, ddfv, &delta)) { *iters = it; return -1; }
+        *x += delta;
+        it += 1;
+        if (it > KEPLER_MAXITER) { *iters = it; return -2; }
+    } while (fabs(delta) > KeplerTol<R>::v());
+    *iters = it;
+    if (sgn(*x) != sgn(x0)) return -3;
+    return 0;
+}
+
+// FP32 Stumpff c0..c3 for the mixed form's first stage.  For |z| < 1 the
+// closed forms (cos w - 1) / z and (sin w / w - 1) / z lose most of FP32's
+// digits to cancellation; there c2 and c3 come from their power series
+// c_k(z) = sum_n z^n / (2n + k)! (positive z is the hyperbolic branch, as
+// in the closed forms; eight terms: the next is below 2^-24 relative), and
+// c0 = 1 + z c2, c1 = 1 + z c3.  Elsewhere the closed forms, with cos/sin
+// (cosh/sinh) evaluated once.
+__device__ __forceinline__ void stumpff_all_f32(float z, float *c)
+{
+    if (fabsf(z) < 1.0f) {
+        // Horner from the eighth term: c2 = 1/2! + z/4! + z^2/6! + ...,
+        // c3 = 1/3! + z/5! + z^2/7! + ...
+        float c2 = 1.0f / 20922789888000.0f;   // 1/16!
+        float c3 = 1.0f / 355687428096000.0f;  // 1/17!
+        c2 = __fmaf_rn(c2, z, 1.0f / 87178291200.0f);    // 1/14!
+        c3 = __fmaf_rn(c3, z, 1.0f / 1307674368000.0f);  // 1/15!
+        c2 = __fmaf_rn(c2, z, 1.0f / 479001600.0f);      // 1/12!
+        c3 = __fmaf_rn(c3, z, 1.0f / 6227020800.0f);     // 1/13!
+        c2 = __fmaf_rn(c2, z, 1.0f / 3628800.0f);        // 1/10!
+        c3 = __fmaf_rn(c3, z, 1.0f / 39916800.0f);       // 1/11!
+        c2 = __fmaf_rn(c2, z, 1.0f / 40320.0f);          // 1/8!
+        c3 = __fmaf_rn(c3, z, 1.0f / 362880.0f);         // 1/9!
+        c2 = __fmaf_rn(c2, z, 1.0f / 720.0f);            // 1/6!
+        c3 = __fmaf_rn(c3, z, 1.0f / 5040.0f);           // 1/7!
+        c2 = __fmaf_rn(c2, z, 1.0f / 24.0f);             // 1/4!
+        c3 = __fmaf_rn(c3, z, 1.0f / 120.0f);            // 1/5!
+        c2 = __fmaf_rn(c2, z, 0.5f);                     // 1/2!
+        c3 = __fmaf_rn(c3, z, 1.0f / 6.0f);              // 1/3!
+        c[0] = __fmaf_rn(z, c2, 1.0f);
+        c[1] = __fmaf_rn(z, c3, 1.0f);
+        c[2] = c2;
+        c[3] = c3;
+    } else if (z < 0.0f) {
+        const float w = sqrtf(-z);
+        float sw, cw;
+        sincosf(w, &sw, &cw);
+        const float s1 = sw / w;
+        c[0] = cw;
+        c[1] = s1;
+        c[2] = (cw - 1.0f) / z;
+        c[3] = (s1 - 1.0f) / z;
+    } else {
+        const float w = sqrtf(z);
+        const float cw = coshf(w), sw = sinhf(w);
+        const float s1 = sw / w;
+        c[0] = cw;
+        c[1] = s1;
+        c[2] = (cw - 1.0f) / z;
+        c[3] = (s1 - 1.0f) / z;
+    }
+}
+
+// FP32 Laguerre updates from x0 until |delta| <= 2^-20 |x| (FP32 cannot
+// resolve the root much better: f is a difference of terms of size dt).
+// Returns 0, or -1 / -2 (vanishing denominator or a value that is not
+// finite, no convergence in 16 updates).
+__device__ inline int kep_laguerre_f32(float x0, float *x,
+                                       const KepArg<float> &k, int *iters)
+{
+    int it = 0;
+    float s = x0, delta;
+    const float b = k.m + k.al * k.r0;
+    do {
+        float c[4];
+        const float s2 = s * s;
+        stumpff_all_f32(k.al * s2, c);
+        const float S1 = s * c[1], S2 = s2 * c[2], S3 = (s * s2) * c[3];
+        const float fv = __fmaf_rn(k.r0, s, __fmaf_rn(k.rv0, S2, __fmaf_rn(b, S3, -k.dt)));
+        const float dfv = k.r0 + __fmaf_rn(k.rv0, S1, b * S2);
+        const float ddfv = __fmaf_rn(k.rv0, c[0], b * S1);
+        if (!lag_delta(fv, dfv, ddfv, &delta) || !isfinite(delta)) {
+            *iters = it;
+            return -1;
+        }
+        s += delta;
+        it += 1;
+        if (it >= 16) { *iters = it; return -2; }
+    } while (fabsf(delta) > 9.5367431640625e-7f * fabsf(s));   // 2^-20
+    *x = s;
+    *iters = it;
+    return 0;
+}
+
+// KEP_MIXED root: FP32 stage from x0, then FP64 Laguerre updates.  An FP64
+// update d is accepted when |d| <= 2^-42 (the reference's rule) or when the
+// next update it predicts, |f'' / (2 f')| d^2 (Newton's quadratic bound;
+// Laguerre's order-5 update converges at least as fast), is below a quarter
+// of 2^-42: the root then lies within that bound of the reference's.
+// S[1..3] receive S1..S3 at the root, shifted from the last evaluation point
+// by their Taylor series in d (dS_{k+1}/ds = S_k, dS_0/ds = al S_1) to
+// second order (d is FP32-small, so the third-order term is below double
+// rounding).
+__device__ inline int kep_laguerre_mixed(double x0, double *x,
+                                         const KepArg<double> &k, int *iters,
+                                         int *iters32, double *S)
+{
+    const double tol = KeplerTol<double>::v();
+    KepArg<float> kf = {(float)k.dt, (float)k.r0, (float)k.rv0, (float)k.m,
+                        (float)k.al};
+    float xf = 0.f;
+    int n32 = 0;
+    double s = x0;
+    if (kep_laguerre_f32((float)x0, &xf, kf, &n32) == 0 &&
+        sgn((double)xf) == sgn(x0))
+        s = (double)xf;
+    *iters32 = n32;
+    int it = 0;
+    for (;;) {
+        double Sp[4], fv, dfv, ddfv, delta;
+        kep_S(s, k.al, Sp);
+        kep_fdd(Sp, s, k, &fv, &dfv, &ddfv);
+        if (!lag_delta(fv, dfv, ddfv, &delta)) { *iters = it; return -1; }
+        s += delta;
+        it += 1;
+        const bool done =
+            fabs(delta) <= tol ||
+            fabs(ddfv / (2.0 * dfv)) * (delta * delta) <= 0.25 * tol;
+        if (done) {
+            const double d = delta, h = 0.5 * delta * delta;
+            S[1] = Sp[1] + d * Sp[0] + h * (k.al * Sp[1]);
+            S[2] = Sp[2] + d * Sp[1] + h * Sp[0];
+            S[3] = Sp[3] + d * Sp[2] + h * Sp[1];
+            break;
+        }
+        if (it > KEPLER_MAXITER) { *iters = it; return -2; }
+    }
+    *x = s;
+    *iters = it;
+    if (sgn(*x) != sgn(x0)) return -3;
+    return 0;
+}
 
 // Plain first guess of _universal_kepler_solver (:405-425) and the quantities
 // it derives; returns false for a zero separation (no motion, :384-394).
@@ -209,7 +474,31 @@ __device__ int kep_single(R dt0, R m, R e2, R *p, KepCtx<R> &c)
     }
     R s;
     int it = 0;
-    int err = kep_laguerre(s0, &s, ka, &it);
+    int err;
+    if constexpr (sizeof(R) == sizeof(double)) {
+        if (c.form == KEP_MIXED) {
+            R S[4];
+            int it32 = 0;
+            err = kep_laguerre_mixed(s0, &s, ka, &it, &it32, S);
+            c.solves += 1;
+            c.iterations += it;
+            c.iterations32 += it32;
+            if (err == 0) kep_update_S(ka.dt, S, ka.r0, m, e2, p);
+            return err;
+        }
+    }
+    if (c.form == KEP_SHARED) {
+        err = kep_laguerre_shared(s0, &s, ka, &it);
+        c.solves += 1;
+        c.iterations += it;
+        if (err == 0) {
+            R S[4];
+            kep_S(s, ka.al, S);
+            kep_update_S(ka.dt, S, ka.r0, m, e2, p);
+        }
+        return err;
+    }
+    err = kep_laguerre(s0, &s, ka, &it);
     c.solves += 1;
     c.iterations += it;
     if (err == 0) kep_update(ka.dt, s, ka.r0, m, e2, ka.al, p);

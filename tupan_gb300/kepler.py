@@ -23,6 +23,8 @@ def _declare(L):
         c.c_int64, c.POINTER(_VP), c.c_int, c.c_longlong, _VP,
         c.POINTER(c.c_ulonglong), c.POINTER(c.c_longlong), c.c_int]
     L.tupan_gb300_sakura_queue.restype = c.c_int
+    L.tupan_gb300_kepler_set_form.argtypes = [c.c_int]
+    L.tupan_gb300_kepler_set_form.restype = c.c_int
 
 
 def _lib():
@@ -68,6 +70,20 @@ def kepler_pairs(n, dt, m, e2, state, out, iters=None, rec_x=None,
         int(budget), stream)
     if st:
         raise lib.TupanGB300Error("kepler_pairs failed: status %d" % st)
+
+
+FORMS = {"reference": 0, "shared": 1, "mixed": 2}
+
+
+def set_form(form):
+    """Root-solve form of the pair solver and the Sakura paths: "reference"
+    (the reference's structure), "shared" (one cos/sin per Laguerre update,
+    bit-identical) or "mixed" (FP32 updates, then FP64 to the reference's
+    tolerance).  Returns the previous form's name."""
+    old = _lib().tupan_gb300_kepler_set_form(FORMS[form])
+    if old < 0:
+        raise ValueError(form)
+    return {v: k for k, v in FORMS.items()}[old]
 
 
 def set_mlp(w1, b1, w2, b2, w3, b3, norm, gate=float("-inf")):
