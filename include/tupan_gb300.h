@@ -160,7 +160,8 @@ unsigned tupan_gb300_last_device_error(void);
 /* Arithmetic mode: 0 EXACT (default; bit-identical to the reference C for all
  * kernels but Sakura/Kepler, which agree to libm accuracy), 1 SPLIT (FP32
  * pairs on double-single positions with compensated sums; float64 library,
- * kernels phi/acc/acc_jerk/snap_crackle/tstep -- the others stay EXACT).
+ * kernels phi/acc/acc_jerk/snap_crackle/tstep/pnacc -- the others stay
+ * EXACT).
  * Returns the previous mode.  The environment variable TUPAN_GB300_MODE=split
  * selects SPLIT at load time. */
 int tupan_gb300_set_mode(int mode);

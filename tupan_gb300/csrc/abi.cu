@@ -53,6 +53,11 @@ cudaError_t launch_split(int kernel, const float4 *irec, const float4 *jrec,
                          uint64_t ni, uint64_t nj, void *const *out,
                          double *partial, int variant, int gsplit, double eta,
                          unsigned *err, cudaStream_t st);
+cudaError_t launch_split_pn(int kernel, const float4 *irec,
+                            const float4 *jrec, uint64_t ni, uint64_t nj,
+                            void *const *out, double *partial, int variant,
+                            int gsplit, double eta, const double *pn,
+                            unsigned *err, cudaStream_t st);
 int split_variant_count();
 void split_variant_info(int v, int *ni_per_thread, int *jsplit, int *threads);
 bool split_supported(int kernel);
@@ -345,8 +350,10 @@ int run_device_sweep(DeviceState *d, Sweep &s, cudaStream_t st)
                   "partial buffer");
         if (rc) return rc;
     }
-    e = launch_split(k, irec, jrec, s.ni, s.nj, s.out, d->partial, variant,
-                     gsplit, s.scal[0], d->err, st);
+    double pn[8] = {(double)s.iscal, s.scal[1], s.scal[2], s.scal[3],
+                    s.scal[4], s.scal[5], s.scal[6], s.scal[7]};
+    e = launch_split_pn(k, irec, jrec, s.ni, s.nj, s.out, d->partial, variant,
+                        gsplit, s.scal[0], pn, d->err, st);
     if (e != cudaSuccess) return cuda_fail(e, "split sweep launch");
     return ST_OK;
 #else

@@ -17,13 +17,102 @@
 // The j - i sign convention is used throughout (the reference forms i - j
 // and subtracts); every output is the same quantity.
 
+#include <string.h>
+
 #include <type_traits>
 
 #include "tg_common.cuh"
+#include "tg_pn.cuh"
 #include "tg_split_ops.cuh"
 #include "tg_tma.cuh"
 
 namespace tg {
+
+// Post-Newtonian order and inverse powers of c for the PNAcc sweep.
+struct PnParams {
+    int order;
+    float inv[8];   // inv[k] = 1/c^k, k = 1..7
+};
+
+// pnacc_kernel_common.h:8-70 with p2p_pnterms (pn_terms.h:473-567) in FP32:
+// the reference's PN polynomials (tg_pn.cuh, instantiated in float) on the
+// double-single position difference, softened 1/r from rsqrt.  The result
+// is the PN correction alone, as in the reference; i - j as there.
+struct PnAccS {
+    static constexpr int NF = 3, NO = 3, MAXC = -1;
+    static constexpr bool PN = true;
+    using P = PosVelRec;
+    __device__ static P load(const float4 *r) { return AccJerkS::load(r); }
+    __device__ static void pair(const P &i, const P &j, float *o,
+                                const PnParams &pn)
+    {
+        const float im = i.m, jm = j.m;
+        const float dx = (i.xh - j.xh) + (i.xl - j.xl);
+        const float dy = (i.yh - j.yh) + (i.yl - j.yl);
+        const float dz = (i.zh - j.zh) + (i.zl - j.zl);
+        const float h2 = i.e2 + j.e2;
+        const float ux = i.vx - j.vx, uy = i.vy - j.vy, uz = i.vz - j.vz;
+        const float r2 = fmaf(dz, dz, fmaf(dy, dy, dx * dx));
+        const float v2 = fmaf(uz, uz, fmaf(uy, uy, ux * ux));
+        float inv_r = rsqrtf(r2 + h2);
+        inv_r = (r2 > 0.f) ? inv_r : 0.f;      // self pairs contribute nothing
+        const float inv_r2 = inv_r * inv_r;
+        const float inv_r3 = inv_r2 * inv_r;
+        const float nx = dx * inv_r, ny = dy * inv_r, nz = dz * inv_r;
+        const float iv2 = fmaf(i.vz, i.vz, fmaf(i.vy, i.vy, i.vx * i.vx));
+        const float jv2 = fmaf(j.vz, j.vz, fmaf(j.vy, j.vy, j.vx * j.vx));
+        PnTerm<float> p2 = {0, 0}, p4 = {0, 0}, p5 = {0, 0}, p6 = {0, 0},
+                      p7 = {0, 0};
+        const int order = pn.order;
+        if (order > 1) {
+            const float niv = fmaf(nz, i.vz, fmaf(ny, i.vy, nx * i.vx));
+            const float njv = fmaf(nz, j.vz, fmaf(ny, j.vy, nx * j.vx));
+            const float njv2 = njv * njv;
+            const float ivjv = fmaf(i.vz, j.vz, fmaf(i.vy, j.vy, i.vx * j.vx));
+            p2 = pn2<float>(im, jm, inv_r, iv2, jv2, ivjv, niv, njv, njv2,
+                            pn.inv[2]);
+            if (order > 3) {
+                const float im2 = im * im, jm2 = jm * jm, imjm = im * jm;
+                const float jv4 = jv2 * jv2;
+                const float ivjvivjv = ivjv * ivjv;
+                const float nv = fmaf(nz, uz, fmaf(ny, uy, nx * ux));
+                const float niv2 = niv * niv;
+                const float nivnjv = niv * njv;
+                p4 = pn4<float>(im, jm, im2, jm2, imjm, inv_r, inv_r2, iv2,
+                                jv2, jv4, ivjv, ivjvivjv, nv, niv, njv, niv2,
+                                njv2, nivnjv, pn.inv[4]);
+                if (order > 4) {
+                    p5 = pn5<float>(im, jm, inv_r, v2, nv, pn.inv[5]);
+                    if (order > 5) {
+                        const float nvnv = nv * nv;
+                        p6 = pn6<float>(im, jm, im2, jm2, imjm, inv_r, inv_r2,
+                                        v2, iv2, jv2, jv4, ivjv, ivjvivjv, nv,
+                                        nvnv, niv, njv, niv2, njv2, nivnjv,
+                                        pn.inv[6]);
+                        if (order > 6) {
+                            const float iv4 = iv2 * iv2;
+                            p7 = pn7<float>(im, jm, im2, jm2, imjm, inv_r,
+                                            inv_r2, v2, iv2, jv2, iv4, jv4,
+                                            ivjv, nv, nvnv, niv, njv, niv2,
+                                            njv2, nivnjv, pn.inv[7]);
+                        }
+                    }
+                }
+            }
+        }
+        const float pa = ((((p7.a + p6.a) + p5.a) + p4.a) + p2.a) * (jm * inv_r3);
+        const float pb = ((((p7.b + p6.b) + p5.b) + p4.b) + p2.b) * (jm * inv_r2);
+        o[0] = fmaf(pa, dx, fmaf(pb, ux, o[0]));
+        o[1] = fmaf(pa, dy, fmaf(pb, uy, o[1]));
+        o[2] = fmaf(pa, dz, fmaf(pb, uz, o[2]));
+    }
+    __device__ static void finish(double *, double) {}
+};
+
+// Whether an operator takes the PN parameters instead of eta.
+template <class Op, class = void> struct TakesPn : std::false_type {};
+template <class Op>
+struct TakesPn<Op, std::void_t<decltype(Op::PN)>> : std::true_type {};
 
 // ---------------------------------------------------------------------------
 // Packed FP32 particle records (float4 units):
@@ -93,6 +182,7 @@ struct SplitLaunch {
     double eta_d;
     unsigned *err;
     uint32_t spin;        // main-loop wait limit (pipe_spin_limit())
+    PnParams pn;          // PNAcc only
 };
 
 constexpr int SPLIT_TILE = 256;   // j-records per pipeline stage
@@ -270,8 +360,12 @@ split_sweep(const SplitLaunch L)
                     const typename Op::P jp =
                         Op::load(tile + (r0 + u * JS + js) * NF);
 #pragma unroll
-                    for (int k = 0; k < NI; ++k)
-                        Op::pair(ip[k], jp, part[k], L.eta);
+                    for (int k = 0; k < NI; ++k) {
+                        if constexpr (TakesPn<Op>::value)
+                            Op::pair(ip[k], jp, part[k], L.pn);
+                        else
+                            Op::pair(ip[k], jp, part[k], L.eta);
+                    }
                 }
                 fold();
             }
@@ -280,8 +374,12 @@ split_sweep(const SplitLaunch L)
             for (int r = js; r < n; r += JS) {
                 const typename Op::P jp = Op::load(tile + r * NF);
 #pragma unroll
-                for (int k = 0; k < NI; ++k)
-                    Op::pair(ip[k], jp, part[k], L.eta);
+                for (int k = 0; k < NI; ++k) {
+                    if constexpr (TakesPn<Op>::value)
+                        Op::pair(ip[k], jp, part[k], L.pn);
+                    else
+                        Op::pair(ip[k], jp, part[k], L.eta);
+                }
             }
             fold();
         }
@@ -425,7 +523,7 @@ bool split_has_x2(int kernel)
 bool split_supported(int kernel)
 {
     return kernel == K_PHI || kernel == K_ACC || kernel == K_ACC_JERK ||
-           kernel == K_TSTEP || kernel == K_SNAP_CRACKLE;
+           kernel == K_TSTEP || kernel == K_SNAP_CRACKLE || kernel == K_PNACC;
 }
 
 template <class Op, int NI, int JS, int NT, int MINB, bool X2 = false>
@@ -489,10 +587,27 @@ static cudaError_t run_op(const SplitLaunch &L, int variant, int gsplit,
 
 // irec/jrec: packed records (launch_pack); out: NO double arrays;
 // partial: gsplit x NO x ni doubles when gsplit > 1.
+cudaError_t launch_split_pn(int kernel, const float4 *irec,
+                            const float4 *jrec, uint64_t ni, uint64_t nj,
+                            void *const *out, double *partial, int variant,
+                            int gsplit, double eta, const double *pn,
+                            unsigned *err, cudaStream_t st);
+
 cudaError_t launch_split(int kernel, const float4 *irec, const float4 *jrec,
                          uint64_t ni, uint64_t nj, void *const *out,
                          double *partial, int variant, int gsplit, double eta,
                          unsigned *err, cudaStream_t st)
+{
+    return launch_split_pn(kernel, irec, jrec, ni, nj, out, partial, variant,
+                           gsplit, eta, nullptr, err, st);
+}
+
+// As launch_split; pn: PN order then 1/c .. 1/c^7 (PNAcc; else unused).
+cudaError_t launch_split_pn(int kernel, const float4 *irec,
+                            const float4 *jrec, uint64_t ni, uint64_t nj,
+                            void *const *out, double *partial, int variant,
+                            int gsplit, double eta, const double *pn,
+                            unsigned *err, cudaStream_t st)
 {
     if (ni == 0) return cudaSuccess;
     if (gsplit < 1) gsplit = 1;
@@ -512,12 +627,18 @@ cudaError_t launch_split(int kernel, const float4 *irec, const float4 *jrec,
     L.eta_d = eta;
     L.err = err;
     L.spin = pipe_spin_limit();
+    memset(&L.pn, 0, sizeof(L.pn));
+    if (pn) {
+        L.pn.order = (int)pn[0];
+        for (int q = 1; q < 8; ++q) L.pn.inv[q] = (float)pn[q];
+    }
     switch (kernel) {
     case K_PHI: return run_op<PhiS>(L, variant, gsplit, st);
     case K_ACC: return run_op<AccS>(L, variant, gsplit, st);
     case K_ACC_JERK: return run_op<AccJerkS>(L, variant, gsplit, st);
     case K_TSTEP: return run_op<TstepS>(L, variant, gsplit, st);
     case K_SNAP_CRACKLE: return run_op<SnapS>(L, variant, gsplit, st);
+    case K_PNACC: return run_op<PnAccS>(L, variant, gsplit, st);
     default: return cudaErrorInvalidValue;
     }
 }
