@@ -31,15 +31,30 @@ _LOCK = threading.Lock()
 _LIBS = {}
 
 
+def reference_root():
+    """The reference tree: $TUPAN_REFERENCE, else the one the recipe
+    (oracle/Makefile) names.  None when it is not present."""
+    root = os.environ.get("TUPAN_REFERENCE")
+    if not root:
+        try:
+            root = subprocess.run(["make", "-s", "-C", HERE, "print-reference"],
+                                  stdout=subprocess.PIPE,
+                                  stderr=subprocess.DEVNULL, text=True,
+                                  check=True).stdout.strip()
+        except (OSError, subprocess.CalledProcessError):
+            return None
+    return root if root and os.path.isdir(os.path.join(root, "tupan")) \
+        else None
+
+
 def build(ref=False):
     """Compile the oracle (and, if asked and available, the reference)."""
     subprocess.check_call(["make", "-s", "-C", HERE, "all"])
     if ref:
-        src = os.environ.get("TUPAN_REFERENCE_SRC",
-                             "/root/reference/tupan/lib/src")
-        if os.path.isdir(src):
+        root = reference_root()
+        if root:
             subprocess.check_call(["make", "-s", "-C", HERE, "ref",
-                                   "REFSRC=" + src])
+                                   "TUPAN_REFERENCE=" + root])
 
 
 def _load(path):

@@ -2,7 +2,7 @@
 
 Run (needs the reference source tree; it is imported, never copied):
 
-    HOME=$PWD/_work/home python tests/golden/make_golden.py /path/to/reference
+    HOME=<a writable directory> python tests/golden/make_golden.py <reference tree>
 
 The script imports ``tupan.lib.extensions`` from the reference, which builds
 the reference's own C kernels through its cffi backend
@@ -506,7 +506,10 @@ def sia(refroot):
 
 
 if __name__ == "__main__":
-    ref = sys.argv[1] if len(sys.argv) > 1 else "/root/reference"
+    if len(sys.argv) < 2 or sys.argv[1].startswith("--"):
+        sys.exit("usage: make_golden.py <reference tree> [--integrators|"
+                 "--sia|--config1|--nreg|--plummer|--tiny]")
+    ref = sys.argv[1]
     if "--integrators" in sys.argv:
         integrators(ref)
     elif "--sia" in sys.argv:

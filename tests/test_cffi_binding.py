@@ -8,12 +8,13 @@ import os
 
 import pytest
 
+import oracle
 from tupan_gb300 import lib
 
 cffi = pytest.importorskip("cffi")
 
-REF_H = os.path.join(os.environ.get("TUPAN_REFERENCE", "/root/reference"),
-                     "tupan", "lib", "src", "libtupan.h")
+_ROOT = oracle.reference_root()
+REF_H = os.path.join(_ROOT or "", "tupan", "lib", "src", "libtupan.h")
 NAMES = ("phi_kernel", "acc_kernel", "acc_jerk_kernel", "snap_crackle_kernel",
          "tstep_kernel", "pnacc_kernel", "nreg_Xkernel", "nreg_Vkernel",
          "sakura_kernel", "kepler_solver_kernel")

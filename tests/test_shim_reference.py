@@ -12,8 +12,10 @@ import sys
 
 import pytest
 
+import oracle
+
 ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
-REF = os.environ.get("TUPAN_REFERENCE", "/root/reference")
+REF = oracle.reference_root() or ""
 
 CHILD = r"""
 import json, sys
