@@ -318,6 +318,15 @@ int tupan_gb300_block_get_state(void *handle, double *rx, double *ry,
                                 double *rz, double *vx, double *vy,
                                 double *vz, double *t, double *dt);
 int tupan_gb300_block_destroy(void *handle);
+/* How block steps are launched: 1 (default) one CUDA graph per batch of
+ * steps, the active set sized on the device (a WHILE node over steps, a
+ * SWITCH node over active-count levels whose bodies are captured with the
+ * sweep shape of each level); 0 host-synchronised (the active count is read
+ * back every step).  Returns the previous setting, -1 for a null handle. */
+int tupan_gb300_block_set_graphs(void *handle, int on);
+/* 1 when evolve runs the graph path, 0 the host-synchronised one (also when
+ * the graph could not be built). */
+int tupan_gb300_block_launch_mode(void *handle);
 
 /* ------------------------------------------------------------------------
  * Sakura and Kepler (libtupan_gb300.so only).  The pair arithmetic is that

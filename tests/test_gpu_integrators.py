@@ -90,8 +90,12 @@ def test_split_hermite4_energy_and_steps():
 from tupan_gb300.integrator import DeviceBlockHermite  # noqa: E402
 
 
+@pytest.mark.parametrize("graphs", [True, False])
 @pytest.mark.parametrize("order", [4, 6, 8])
-def test_exact_block_steps_bit_identical_to_oracle(order):
+def test_exact_block_steps_bit_identical_to_oracle(order, graphs):
+    # graphs: the steps run as CUDA graphs with the active set sized on the
+    # device (WHILE over steps, SWITCH over active-count levels); else the
+    # active count is read back each step
     ps = ics.plummer(96, eps=1e-4, seed=40 + order, masses="salpeter")
     eta, dt_max = 1.0 / 32, 1.0 / 16
     st = oi.block_init(ps, order, eta, dt_max)
@@ -100,10 +104,36 @@ def test_exact_block_steps_bit_identical_to_oracle(order):
         t, na = oi.block_step(st, order, eta, dt_max)
         active.append(na)
     assert min(active) < len(ps["m"])          # the sets really vary
-    b = DeviceBlockHermite(ps, eta, dt_max, order=order, mode="exact")
+    b = DeviceBlockHermite(ps, eta, dt_max, order=order, mode="exact",
+                           graphs=graphs)
     b.evolve(1e30, max_steps=40)
+    assert b.launch_mode == ("graphs" if graphs else "host")
+    assert b.nsteps == 40
     assert b.time == t
     assert b.active == sum(active)
+    got = b.state()
+    for k in ("rx", "ry", "rz", "vx", "vy", "vz", "t", "dt"):
+        np.testing.assert_array_equal(got[k], st[k], err_msg=k)
+    b.close()
+
+
+def test_block_steps_switch_between_launch_paths():
+    # 15 steps on the graph path, 10 host-synchronised, 15 more on graphs:
+    # the device-side block time and counters follow the host's
+    ps = ics.plummer(200, eps=1e-4, seed=47, masses="salpeter")
+    eta, dt_max, order = 1.0 / 32, 1.0 / 16, 4
+    st = oi.block_init(ps, order, eta, dt_max)
+    total = 0
+    for _ in range(40):
+        t, na = oi.block_step(st, order, eta, dt_max)
+        total += na
+    b = DeviceBlockHermite(ps, eta, dt_max, order=order, mode="exact")
+    b.evolve(1e30, max_steps=15)
+    b.L.tupan_gb300_block_set_graphs(b.h, 0)
+    b.evolve(1e30, max_steps=10)
+    b.L.tupan_gb300_block_set_graphs(b.h, 1)
+    b.evolve(1e30, max_steps=15)
+    assert b.nsteps == 40 and b.time == t and b.active == total
     got = b.state()
     for k in ("rx", "ry", "rz", "vx", "vy", "vz", "t", "dt"):
         np.testing.assert_array_equal(got[k], st[k], err_msg=k)

@@ -25,6 +25,7 @@ def main(argv=None):
     ap.add_argument("--eta", type=float, default=1.0 / 32)
     ap.add_argument("--dt-max", type=float, default=1.0 / 32)
     ap.add_argument("--mode", default="split")
+    ap.add_argument("--launch", default="graphs", choices=["graphs", "host"])
     a = ap.parse_args(argv)
 
     from . import ics
@@ -35,11 +36,13 @@ def main(argv=None):
     k0, p0 = e0.energy()
     e0.close()
     t0 = time.perf_counter()
-    b = DeviceBlockHermite(ps, a.eta, a.dt_max, order=a.order, mode=a.mode)
+    b = DeviceBlockHermite(ps, a.eta, a.dt_max, order=a.order, mode=a.mode,
+                           graphs=a.launch == "graphs")
     t1 = time.perf_counter()
     b.evolve(a.t_end)
     t2 = time.perf_counter()
     st = b.state()
+    launch = b.launch_mode
     b.close()
     fin = dict(ps)
     fin.update({k: st[k] for k in ("rx", "ry", "rz", "vx", "vy", "vz")})
@@ -48,6 +51,7 @@ def main(argv=None):
     e1.close()
     sweeps = 3 if a.order == 4 else 5        # acc_jerk x2 (+ snap x2) + tstep
     res = {"n": a.n, "order": a.order, "mode": a.mode, "t_end": a.t_end,
+           "launch": launch,
            "time": b.time, "block_steps": b.nsteps,
            "active_updates": b.active,
            "mean_active": b.active / max(b.nsteps, 1),

@@ -20,6 +20,16 @@
 // everything else, so small sets use the j-split variants.  All fp64 updates
 // are compiled without contraction; with EXACT forces a run is bit-identical
 // to the numpy restatement of the scheme used by the tests.
+//
+// Launching.  The size of the active set is decided on the GPU each step.
+// By default the steps run as one CUDA graph per batch of steps with no host
+// round trip: a WHILE node repeats the block step while the block time is
+// below t_end (at most a step budget per launch); inside it, after the
+// active set is selected, a SWITCH node picks one of the bodies captured per
+// block level -- level L holds active counts in (2^(L-1), 2^L] -- whose
+// sweeps have the launch shape chosen for 2^L particles and read the exact
+// count on the device (CTAs past it leave at once).  The host-synchronised
+// path (read the count back, then launch for it) stays available.
 
 #include <cuda_runtime.h>
 #include <math.h>
@@ -40,6 +50,15 @@ cudaError_t launch_split(int kernel, const float4 *irec, const float4 *jrec,
                          uint64_t ni, uint64_t nj, void *const *out,
                          double *partial, int variant, int gsplit, double eta,
                          unsigned *err, cudaStream_t st);
+cudaError_t launch_pack_dev(int kernel, uint64_t n, const unsigned *n_dev,
+                            const void *const *attrs, float4 *out,
+                            cudaStream_t st);
+cudaError_t launch_split_dev(int kernel, const float4 *irec,
+                             const float4 *jrec, uint64_t ni,
+                             const unsigned *ni_dev, uint64_t nj,
+                             void *const *out, double *partial, int variant,
+                             int gsplit, double eta, const double *pn,
+                             unsigned *err, cudaStream_t st);
 void choose_split_public(int kernel, uint64_t ni, uint64_t nj, int *variant,
                          int *gsplit);
 }  // namespace tg
@@ -48,10 +67,21 @@ using namespace tg;
 
 namespace {
 
+constexpr int MAX_LEVELS = 40;   // active-count levels of the graph path
+
 struct BlockCtl {
     unsigned long long t_next_bits;   // min (t_i + dt_i), ordered bits
     unsigned int count;               // active particles
-    unsigned int pad;
+    unsigned int stalled;             // a step did not advance the block time
+    // graph path: state kept on the device between steps
+    double t_last;                    // block time of the last step
+    double t_end;
+    long long nsteps, active_sum;
+    long long steps_left;             // step budget of the current launch
+    unsigned long long launches;      // kernels run by the graph's steps
+    int level;                        // level chosen for the current step
+    int pad2;
+    unsigned long long level_launches[MAX_LEVELS + 1];   // per level body
 };
 
 // Per-particle state (SoA, fp64, N each).
@@ -239,6 +269,61 @@ __global__ void k_new_dt(BState S, const BlockCtl *c, double dt_max)
     }
 }
 
+// Level of an active count: L with count in (2^(L-1), 2^L]; 0 for 1.
+__device__ __forceinline__ int count_level(unsigned count)
+{
+    return count <= 1u ? 0 : 32 - __clz(count - 1u);
+}
+
+// Graph path: choose the level body of this step (none for an empty set).
+__global__ void k_level(BlockCtl *c, cudaGraphConditionalHandle hs, int nb)
+{
+    if (threadIdx.x != 0) return;
+    const unsigned count = c->count;
+    const int lv = count ? count_level(count) : nb;
+    c->level = lv;
+    cudaGraphSetConditional(hs, (unsigned)(lv < nb ? lv : nb));
+}
+
+// Graph path: close the step (statistics, block time) and decide whether the
+// WHILE node runs another: the block time advanced, is still below t_end and
+// the launch's step budget is not spent.  `pre` kernels ran before the level
+// body and this one.
+__global__ void k_step_end(BlockCtl *c, cudaGraphConditionalHandle hw,
+                           int nb, unsigned long long pre)
+{
+    if (threadIdx.x != 0) return;
+    const double tn = __longlong_as_double((long long)c->t_next_bits);
+    const unsigned count = c->count;
+    bool progress = false;
+    if (count > 0 && tn > c->t_last) {
+        progress = true;
+        c->nsteps += 1;
+        c->active_sum += count;
+        c->t_last = tn;
+    }
+    if (!progress) c->stalled = 1;
+    c->launches += pre + (c->level < nb ? c->level_launches[c->level] : 0ull);
+    c->steps_left -= 1;
+    const bool more = progress && c->t_last < c->t_end && c->steps_left > 0;
+    cudaGraphSetConditional(hw, more ? 1u : 0u);
+}
+
+// Graph path: arm a launch (end time, step budget, and the host's view of
+// the block time and counters, which the host-synchronised path may have
+// advanced).
+__global__ void k_arm(BlockCtl *c, double t_end, long long steps,
+                      double t_last, long long nsteps, long long active_sum)
+{
+    if (threadIdx.x != 0) return;
+    c->t_end = t_end;
+    c->steps_left = steps;
+    c->stalled = 0;
+    c->t_last = t_last;
+    c->nsteps = nsteps;
+    c->active_sum = active_sum;
+}
+
 __global__ void k_init_dt(BState S, uint64_t n, double dt_max)
 {
     GRID_LOOP(i, n)
@@ -264,6 +349,13 @@ struct Block {
     BState S;
     float4 *pack_i = nullptr, *pack_j = nullptr;
     double *partial = nullptr;
+    // graph path
+    int use_graphs = 1;           // 1: graph path, 0: host-synchronised
+    bool graph_failed = false;    // building the graph failed: host path
+    cudaGraphExec_t exec = nullptr;
+    int nlevels = 0;
+    const unsigned *count_dev = nullptr;   // &ctl->count while capturing
+    unsigned long long host_launches = 0;  // ctl->launches already counted
 };
 
 unsigned grid_for(uint64_t n, int sms)
@@ -290,15 +382,20 @@ cudaError_t bsweep(Block *b, int kernel, uint64_t ni, const double *const *ia,
     }
     for (int o = 0; o < n_out(kernel); ++o) s.out[o] = out[o];
     s.scal[0] = eta;
+    // while a level body is captured, ni is the level's bound and the count
+    // is read on the device
+    s.ni_dev = b->count_dev;
     if (b->mode == MODE_EXACT)
         return launch_exact<double>(s, b->stream, 1LL << 20, b->err);
-    cudaError_t e = launch_pack(kernel, ni, s.ip, b->pack_i, b->stream);
+    cudaError_t e = launch_pack_dev(kernel, ni, b->count_dev, s.ip, b->pack_i,
+                                    b->stream);
     if (e == cudaSuccess) e = launch_pack(kernel, b->n, s.jp, b->pack_j, b->stream);
     if (e != cudaSuccess) return e;
     int variant, gsplit;
     choose_split_public(kernel, ni, b->n, &variant, &gsplit);
-    return launch_split(kernel, b->pack_i, b->pack_j, ni, b->n, s.out,
-                        b->partial, variant, gsplit, eta, b->err, b->stream);
+    return launch_split_dev(kernel, b->pack_i, b->pack_j, ni, b->count_dev,
+                            b->n, s.out, b->partial, variant, gsplit, eta,
+                            nullptr, b->err, b->stream);
 }
 
 // Forces of the ni i-particles given by (m, e2, r, v) arrays against the
@@ -318,6 +415,9 @@ cudaError_t bforces(Block *b, uint64_t ni, const double *im, const double *ie2,
 }
 
 template <int ORDER>
+cudaError_t step_body(Block *b, uint64_t na);
+
+template <int ORDER>
 int block_step(Block *b)
 {
     BState &S = b->S;
@@ -335,31 +435,169 @@ int block_step(Block *b)
         cudaStreamSynchronize(st) != cudaSuccess)
         return ST_CUDA;
     const uint64_t na = c.count;
-    const unsigned ga = grid_for(na, b->sms);
-    for (int pass = 0; pass < 2; ++pass) {
-        if (bforces(b, na, S.cm, S.ce2, S.cr, S.cv, S.cf) != cudaSuccess)
-            return ST_CUDA;
-        k_correct_active<ORDER><<<ga, 256, 0, st>>>(S, b->ctl);
-        g_launch_count += 1;
-    }
-    k_commit<ORDER><<<ga, 256, 0, st>>>(S, b->ctl);
-    g_launch_count += 1;
-    {
-        const double *ia[8] = {S.cm, S.cr[0], S.cr[1], S.cr[2], S.ce2,
-                               S.cv[0], S.cv[1], S.cv[2]};
-        const double *ja[8] = {S.m, S.rp[0], S.rp[1], S.rp[2], S.e2,
-                               S.vp[0], S.vp[1], S.vp[2]};
-        if (bsweep(b, K_TSTEP, na, ia, ja, S.cdt, b->eta) != cudaSuccess)
-            return ST_CUDA;
-    }
-    k_new_dt<<<ga, 256, 0, st>>>(S, b->ctl, b->dt_max);
-    g_launch_count += 1;
-    if (cudaGetLastError() != cudaSuccess) return ST_CUDA;
+    if (step_body<ORDER>(b, na) != cudaSuccess) return ST_CUDA;
     double tn;
     memcpy(&tn, &c.t_next_bits, sizeof(tn));
     b->t = tn;
     b->nsteps += 1;
     b->active_sum += (long long)na;
+    return ST_OK;
+}
+
+// The forces, corrections, commit and new steps of one block step for an
+// active set of at most `na` particles (count read on the device when
+// count_dev is set).
+template <int ORDER>
+cudaError_t step_body(Block *b, uint64_t na)
+{
+    BState &S = b->S;
+    cudaStream_t st = b->stream;
+    const unsigned ga = grid_for(na, b->sms);
+    for (int pass = 0; pass < 2; ++pass) {
+        cudaError_t e = bforces(b, na, S.cm, S.ce2, S.cr, S.cv, S.cf);
+        if (e != cudaSuccess) return e;
+        k_correct_active<ORDER><<<ga, 256, 0, st>>>(S, b->ctl);
+        g_launch_count += 1;
+    }
+    k_commit<ORDER><<<ga, 256, 0, st>>>(S, b->ctl);
+    g_launch_count += 1;
+    const double *ia[8] = {S.cm, S.cr[0], S.cr[1], S.cr[2], S.ce2,
+                           S.cv[0], S.cv[1], S.cv[2]};
+    const double *ja[8] = {S.m, S.rp[0], S.rp[1], S.rp[2], S.e2,
+                           S.vp[0], S.vp[1], S.vp[2]};
+    cudaError_t e = bsweep(b, K_TSTEP, na, ia, ja, S.cdt, b->eta);
+    if (e != cudaSuccess) return e;
+    k_new_dt<<<ga, 256, 0, st>>>(S, b->ctl, b->dt_max);
+    g_launch_count += 1;
+    return cudaGetLastError();
+}
+
+// Builds the graph path: WHILE { select; SWITCH(level) { body }; end }.
+// Host work only (capture into graphs); nothing runs.
+template <int ORDER>
+cudaError_t build_graph(Block *b)
+{
+    BState &S = b->S;
+    cudaStream_t st = b->stream;
+    const unsigned g = grid_for(b->n, b->sms);
+    int nb = 1;
+    while ((1ull << (nb - 1)) < b->n && nb < MAX_LEVELS) ++nb;
+    b->nlevels = nb;
+    cudaGraph_t G = nullptr;
+    TG_CUDA_TRY(cudaGraphCreate(&G, 0));
+    cudaGraphConditionalHandle hw, hs;
+    cudaError_t e = cudaGraphConditionalHandleCreate(&hw, G, 1,
+                                                     cudaGraphCondAssignDefault);
+    cudaGraphNodeParams wp = {};
+    wp.type = cudaGraphNodeTypeConditional;
+    wp.conditional.handle = hw;
+    wp.conditional.type = cudaGraphCondTypeWhile;
+    wp.conditional.size = 1;
+    cudaGraphNode_t wn;
+    if (e == cudaSuccess) e = cudaGraphAddNode(&wn, G, nullptr, nullptr, 0, &wp);
+    if (e != cudaSuccess) { cudaGraphDestroy(G); return e; }
+    cudaGraph_t W = wp.conditional.phGraph_out[0];
+
+    const unsigned long long c0 = g_launch_count.load();
+    e = cudaStreamBeginCaptureToGraph(st, W, nullptr, nullptr, 0,
+                                      cudaStreamCaptureModeThreadLocal);
+    if (e != cudaSuccess) { cudaGraphDestroy(G); return e; }
+    k_reset<<<1, 1, 0, st>>>(b->ctl);
+    k_next_time<<<g, 256, 0, st>>>(S, b->n, b->ctl);
+    k_select<<<g, 256, 0, st>>>(S, b->n, b->ctl);
+    k_predict_all<ORDER><<<g, 256, 0, st>>>(S, b->n, b->ctl);
+    k_gather<<<g, 256, 0, st>>>(S, b->ctl);
+    cudaStreamCaptureStatus cs;
+    cudaGraph_t cg = nullptr;
+    const cudaGraphNode_t *deps = nullptr;
+    size_t nd = 0;
+    e = cudaStreamGetCaptureInfo(st, &cs, nullptr, &cg, &deps, nullptr, &nd);
+    if (e == cudaSuccess) e = cudaGraphConditionalHandleCreate(&hs, cg, 0, 0);
+    cudaGraphNodeParams sp = {};
+    sp.type = cudaGraphNodeTypeConditional;
+    sp.conditional.handle = hs;
+    sp.conditional.type = cudaGraphCondTypeSwitch;
+    sp.conditional.size = (unsigned)nb;
+    cudaGraphNode_t sn;
+    if (e == cudaSuccess) {
+        k_level<<<1, 32, 0, st>>>(b->ctl, hs, nb);
+        e = cudaStreamGetCaptureInfo(st, &cs, nullptr, &cg, &deps, nullptr, &nd);
+    }
+    if (e == cudaSuccess) e = cudaGraphAddNode(&sn, cg, deps, nullptr, nd, &sp);
+    if (e == cudaSuccess)
+        e = cudaStreamUpdateCaptureDependencies(st, &sn, nullptr, 1,
+                                                cudaStreamSetCaptureDependencies);
+    // reset, next_time, select, predict, gather, level, step_end
+    const unsigned long long pre = 7;
+    if (e == cudaSuccess)
+        k_step_end<<<1, 32, 0, st>>>(b->ctl, hw, nb, pre);
+    cudaGraph_t Wout = nullptr;
+    const cudaError_t e2 = cudaStreamEndCapture(st, &Wout);
+    if (e == cudaSuccess) e = e2;
+    if (e == cudaSuccess) e = cudaGetLastError();
+    // one body per level, its sweeps shaped for the level's largest count
+    unsigned long long per_level[MAX_LEVELS + 1];
+    memset(per_level, 0, sizeof(per_level));
+    b->count_dev = &b->ctl->count;
+    for (int lv = 0; lv < nb && e == cudaSuccess; ++lv) {
+        uint64_t na = 1ull << lv;
+        if (na > b->n) na = b->n;
+        const unsigned long long l0 = g_launch_count.load();
+        e = cudaStreamBeginCaptureToGraph(st, sp.conditional.phGraph_out[lv],
+                                          nullptr, nullptr, 0,
+                                          cudaStreamCaptureModeThreadLocal);
+        if (e != cudaSuccess) break;
+        cudaError_t eb = step_body<ORDER>(b, na);
+        cudaGraph_t bout = nullptr;
+        e = cudaStreamEndCapture(st, &bout);
+        if (e == cudaSuccess) e = eb;
+        per_level[lv] = g_launch_count.load() - l0;
+    }
+    b->count_dev = nullptr;
+    g_launch_count -= g_launch_count.load() - c0;   // nothing ran yet
+    if (e == cudaSuccess) e = cudaGraphInstantiate(&b->exec, G, 0);
+    cudaGraphDestroy(G);
+    if (e != cudaSuccess) {
+        cudaGetLastError();
+        return e;
+    }
+    // the per-level launch counts let the device count the kernels it runs
+    e = cudaMemcpyAsync(b->ctl->level_launches, per_level, sizeof(per_level),
+                        cudaMemcpyHostToDevice, st);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+    return e;
+}
+
+// Graph-path evolution: launches of up to `batch` steps until the block time
+// reaches t_end or max_steps steps are taken.
+int evolve_graph(Block *b, double t_end, long long max_steps)
+{
+    cudaStream_t st = b->stream;
+    long long taken = 0;
+    for (;;) {
+        if (!(b->t < t_end) || (max_steps > 0 && taken >= max_steps)) break;
+        long long budget = 4096;
+        if (max_steps > 0 && max_steps - taken < budget)
+            budget = max_steps - taken;
+        k_arm<<<1, 32, 0, st>>>(b->ctl, t_end, budget, b->t, b->nsteps,
+                                b->active_sum);
+        g_launch_count += 1;
+        if (cudaGraphLaunch(b->exec, st) != cudaSuccess) return ST_CUDA;
+        BlockCtl c;
+        if (cudaMemcpyAsync(&c, b->ctl, sizeof(c), cudaMemcpyDeviceToHost,
+                            st) != cudaSuccess ||
+            cudaStreamSynchronize(st) != cudaSuccess)
+            return ST_CUDA;
+        g_launch_count += c.launches - b->host_launches;
+        b->host_launches = c.launches;
+        taken += c.nsteps - b->nsteps;
+        b->nsteps = c.nsteps;
+        b->active_sum = c.active_sum;
+        // the block time must advance (a zero or non-finite step would loop)
+        if (c.stalled && !(c.t_last > b->t)) return ST_DEVICE;
+        b->t = c.t_last;
+        if (c.stalled) return ST_DEVICE;
+    }
     return ST_OK;
 }
 
@@ -432,6 +670,7 @@ TG_EXPORT int tupan_gb300_block_create(uint64_t n, int order, int mode,
             cudaSuccess)
         return ST_CUDA;
     cudaMemset(b->err, 0, sizeof(unsigned));
+    cudaMemset(b->ctl, 0, sizeof(BlockCtl));
     const double *src[8] = {m, e2, rx, ry, rz, vx, vy, vz};
     double *dst[8] = {S.m, S.e2, S.r[0], S.r[1], S.r[2], S.v[0], S.v[1], S.v[2]};
     for (int k = 0; k < 8; ++k)
@@ -483,6 +722,28 @@ TG_EXPORT int tupan_gb300_block_evolve(void *handle, double t_end,
 {
     Block *b = (Block *)handle;
     if (!b) return ST_BAD_ARGUMENT;
+    if (b->use_graphs && !b->graph_failed && !b->exec) {
+        const cudaError_t e = b->order == 4 ? build_graph<4>(b)
+                            : b->order == 6 ? build_graph<6>(b)
+                                            : build_graph<8>(b);
+        if (e != cudaSuccess) {
+            // conditional graph nodes unavailable: the host-synchronised
+            // path runs instead (tupan_gb300_block_launch_mode reports it)
+            b->graph_failed = true;
+            cudaGetLastError();
+        }
+    }
+    if (b->use_graphs && b->exec) {
+        const int rc = evolve_graph(b, t_end, max_steps);
+        if (rc) return rc;
+        if (cudaStreamSynchronize(b->stream) != cudaSuccess) return ST_CUDA;
+        unsigned herr = 0;
+        cudaMemcpy(&herr, b->err, sizeof(unsigned), cudaMemcpyDeviceToHost);
+        if (t_out) *t_out = b->t;
+        if (steps_out) *steps_out = b->nsteps;
+        if (active_out) *active_out = b->active_sum;
+        return herr ? ST_DEVICE : ST_OK;
+    }
     long long k = 0;
     while (b->t < t_end && (max_steps <= 0 || k < max_steps)) {
         const double t_before = b->t;
@@ -520,11 +781,34 @@ TG_EXPORT int tupan_gb300_block_get_state(void *handle, double *rx, double *ry,
     return ST_OK;
 }
 
+// How block steps are launched: 1 (default) one CUDA graph per batch of
+// steps, the active-set size decided and used on the device (WHILE over
+// steps, SWITCH over active-count levels); 0 host-synchronised (the count is
+// read back each step).  Returns the previous setting.
+TG_EXPORT int tupan_gb300_block_set_graphs(void *handle, int on)
+{
+    Block *b = (Block *)handle;
+    if (!b) return -1;
+    const int old = b->use_graphs;
+    b->use_graphs = on ? 1 : 0;
+    return old;
+}
+
+// The launch path the last evolve used or will use: 1 graphs, 0
+// host-synchronised (also when building the graph failed).
+TG_EXPORT int tupan_gb300_block_launch_mode(void *handle)
+{
+    Block *b = (Block *)handle;
+    if (!b) return -1;
+    return (b->use_graphs && !b->graph_failed) ? 1 : 0;
+}
+
 TG_EXPORT int tupan_gb300_block_destroy(void *handle)
 {
     Block *b = (Block *)handle;
     if (!b) return ST_BAD_ARGUMENT;
     cudaStreamSynchronize(b->stream);
+    if (b->exec) cudaGraphExecDestroy(b->exec);
     cudaFree(b->pool);
     cudaFree(b->S.idx);
     cudaFree(b->ctl);

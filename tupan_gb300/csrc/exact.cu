@@ -24,7 +24,9 @@ exact_sweep(const Sweep s)
 {
     constexpr int NA = Op::NA;
     __shared__ R tile[NA][EXACT_TILE];
-    const uint64_t ni = s.ni, nj = s.nj;
+    const uint64_t ni = s.ni_dev ? (uint64_t)*s.ni_dev : s.ni, nj = s.nj;
+    // blocks past a device-side count have no i (the whole block leaves)
+    if ((uint64_t)blockIdx.x * EXACT_THREADS >= ni) return;
     const uint64_t i = (uint64_t)blockIdx.x * EXACT_THREADS + threadIdx.x;
     const uint64_t ic = i < ni ? i : ni - 1;
     R ip[NA];

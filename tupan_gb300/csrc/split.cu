@@ -128,10 +128,12 @@ struct PackArgs {
     const double *a[MAX_ATTR];
     int na;      // attributes present (5, 8 or 14)
     int nf;      // float4 per record
+    const unsigned *n_dev;   // count read on the device (or null)
 };
 
-__global__ void pack_records(const PackArgs p, uint64_t n, float4 *out)
+__global__ void pack_records(const PackArgs p, uint64_t n_max, float4 *out)
 {
+    const uint64_t n = p.n_dev ? (uint64_t)*p.n_dev : n_max;
     for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n;
          i += (uint64_t)gridDim.x * blockDim.x) {
         float xh, xl, yh, yl, zh, zl;
@@ -152,11 +154,25 @@ __global__ void pack_records(const PackArgs p, uint64_t n, float4 *out)
     }
 }
 
+cudaError_t launch_pack_dev(int kernel, uint64_t n, const unsigned *n_dev,
+                            const void *const *attrs, float4 *out,
+                            cudaStream_t st);
+
 cudaError_t launch_pack(int kernel, uint64_t n, const void *const *attrs,
                         float4 *out, cudaStream_t st)
 {
+    return launch_pack_dev(kernel, n, nullptr, attrs, out, st);
+}
+
+// As launch_pack; with n_dev set, the count is read on the device (n is its
+// upper bound and sizes the grid).
+cudaError_t launch_pack_dev(int kernel, uint64_t n, const unsigned *n_dev,
+                            const void *const *attrs, float4 *out,
+                            cudaStream_t st)
+{
     if (n == 0) return cudaSuccess;
     PackArgs p;
+    p.n_dev = n_dev;
     p.na = n_attr(kernel);
     p.nf = split_nf(kernel);
     for (int a = 0; a < MAX_ATTR; ++a)
@@ -183,6 +199,7 @@ struct SplitLaunch {
     unsigned *err;
     uint32_t spin;        // main-loop wait limit (pipe_spin_limit())
     PnParams pn;          // PNAcc only
+    const unsigned *ni_dev;   // i count read on the device (ni: its bound)
 };
 
 constexpr int SPLIT_TILE = 256;   // j-records per pipeline stage
@@ -212,6 +229,10 @@ split_sweep(const SplitLaunch L)
     const int tid = threadIdx.x;
     const int js = tid % JS;
     const int grp = tid / JS;
+    const uint64_t ni = L.ni_dev ? (uint64_t)*L.ni_dev : L.ni;
+    // CTAs past a device-side count have no i: the whole CTA leaves before
+    // any barrier or copy exists
+    if ((uint64_t)blockIdx.x * IPC >= ni) return;
     const uint64_t ibase = (uint64_t)blockIdx.x * IPC + (uint64_t)grp * NI;
 
     const uint64_t jb = (uint64_t)blockIdx.y * L.jchunk;
@@ -242,7 +263,7 @@ split_sweep(const SplitLaunch L)
 #pragma unroll
     for (int k = 0; k < NI; ++k) {
         uint64_t i = ibase + k;
-        if (i >= L.ni) i = L.ni - 1;
+        if (i >= ni) i = ni - 1;
         ip[k] = Op::load(L.irec + i * NF);
     }
 
@@ -425,7 +446,7 @@ split_sweep(const SplitLaunch L)
             }
         }
         const uint64_t i = ibase + k;
-        if (js == 0 && i < L.ni) {
+        if (js == 0 && i < ni) {
             if (gridDim.y == 1) {
                 Op::finish(v, L.eta_d);
 #pragma unroll
@@ -433,7 +454,7 @@ split_sweep(const SplitLaunch L)
             } else {
 #pragma unroll
                 for (int c = 0; c < NO; ++c)
-                    L.partial[((uint64_t)blockIdx.y * NO + c) * L.ni + i] = v[c];
+                    L.partial[((uint64_t)blockIdx.y * NO + c) * ni + i] = v[c];
             }
         }
     }
@@ -446,14 +467,15 @@ __global__ void split_finalize(const SplitLaunch L, int gsplit)
     constexpr int NO = Op::NO, MAXC = Op::MAXC;
     // a sweep CTA that reported an error left its partials unwritten
     if (*(volatile unsigned *)L.err) return;
+    const uint64_t ni = L.ni_dev ? (uint64_t)*L.ni_dev : L.ni;
     for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
-         i < L.ni; i += (uint64_t)gridDim.x * blockDim.x) {
+         i < ni; i += (uint64_t)gridDim.x * blockDim.x) {
         double v[NO];
 #pragma unroll
         for (int c = 0; c < NO; ++c) {
-            double a = L.partial[(uint64_t)c * L.ni + i];
+            double a = L.partial[(uint64_t)c * ni + i];
             for (int y = 1; y < gsplit; ++y) {
-                double b = L.partial[((uint64_t)y * NO + c) * L.ni + i];
+                double b = L.partial[((uint64_t)y * NO + c) * ni + i];
                 a = (c == MAXC) ? fmax(a, b) : a + b;
             }
             v[c] = a;
@@ -602,12 +624,33 @@ cudaError_t launch_split(int kernel, const float4 *irec, const float4 *jrec,
                            gsplit, eta, nullptr, err, st);
 }
 
+cudaError_t launch_split_dev(int kernel, const float4 *irec,
+                             const float4 *jrec, uint64_t ni,
+                             const unsigned *ni_dev, uint64_t nj,
+                             void *const *out, double *partial, int variant,
+                             int gsplit, double eta, const double *pn,
+                             unsigned *err, cudaStream_t st);
+
 // As launch_split; pn: PN order then 1/c .. 1/c^7 (PNAcc; else unused).
 cudaError_t launch_split_pn(int kernel, const float4 *irec,
                             const float4 *jrec, uint64_t ni, uint64_t nj,
                             void *const *out, double *partial, int variant,
                             int gsplit, double eta, const double *pn,
                             unsigned *err, cudaStream_t st)
+{
+    return launch_split_dev(kernel, irec, jrec, ni, nullptr, nj, out, partial,
+                            variant, gsplit, eta, pn, err, st);
+}
+
+// As launch_split_pn; with ni_dev set, the i count is read on the device
+// when the sweep runs (ni is its upper bound and sizes the grid; CTAs past
+// the count leave at once).
+cudaError_t launch_split_dev(int kernel, const float4 *irec,
+                             const float4 *jrec, uint64_t ni,
+                             const unsigned *ni_dev, uint64_t nj,
+                             void *const *out, double *partial, int variant,
+                             int gsplit, double eta, const double *pn,
+                             unsigned *err, cudaStream_t st)
 {
     if (ni == 0) return cudaSuccess;
     if (gsplit < 1) gsplit = 1;
@@ -627,6 +670,7 @@ cudaError_t launch_split_pn(int kernel, const float4 *irec,
     L.eta_d = eta;
     L.err = err;
     L.spin = pipe_spin_limit();
+    L.ni_dev = ni_dev;
     memset(&L.pn, 0, sizeof(L.pn));
     if (pn) {
         L.pn.order = (int)pn[0];

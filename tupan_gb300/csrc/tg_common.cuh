@@ -113,6 +113,10 @@ struct Sweep {
     void *out[MAX_OUT];
     double scal[8];        // eta | dt | inv1..inv7 (scal[1..7]) for PN
     int64_t iscal;         // flag (Sakura) | order (PNAcc)
+    // When set, the i count is read on the device from here when the sweep
+    // runs (ni is then its upper bound, used for the launch shape): a sweep
+    // over a set whose size the GPU decides, launched without a host sync.
+    const unsigned *ni_dev;
 };
 
 // Launch configuration of the FP32-split sweep, chosen by the autotuner.

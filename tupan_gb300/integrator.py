@@ -128,13 +128,20 @@ def _declare_block(L):
     L.tupan_gb300_block_get_state.restype = c.c_int
     L.tupan_gb300_block_destroy.argtypes = [c.c_void_p]
     L.tupan_gb300_block_destroy.restype = c.c_int
+    L.tupan_gb300_block_set_graphs.argtypes = [c.c_void_p, c.c_int]
+    L.tupan_gb300_block_set_graphs.restype = c.c_int
+    L.tupan_gb300_block_launch_mode.argtypes = [c.c_void_p]
+    L.tupan_gb300_block_launch_mode.restype = c.c_int
 
 
 class DeviceBlockHermite(object):
     """Hermite (order 4, 6 or 8) with individual power-of-two block steps,
     device resident; see csrc/blockstep.cu for the scheme."""
 
-    def __init__(self, ps, eta, dt_max, order=4, mode="split"):
+    def __init__(self, ps, eta, dt_max, order=4, mode="split", graphs=True):
+        """graphs: launch batches of block steps as one CUDA graph (active
+        set sized on the device); False: read the active count back each
+        step and launch for it."""
         self.L = lib.load("float64")
         _declare_block(self.L)
         self.n = len(ps["m"])
@@ -152,6 +159,13 @@ class DeviceBlockHermite(object):
         self.time = 0.0
         self.nsteps = 0
         self.active = 0
+        self.L.tupan_gb300_block_set_graphs(h, 1 if graphs else 0)
+
+    @property
+    def launch_mode(self):
+        """"graphs" or "host" (the path the evolution takes)."""
+        return "graphs" if self.L.tupan_gb300_block_launch_mode(self.h) == 1 \
+            else "host"
 
     def evolve(self, t_end, max_steps=0):
         t = ctypes.c_double()
