@@ -29,6 +29,10 @@ def main(argv=None):
     ap.add_argument("--variant", type=int, default=-1)
     ap.add_argument("--gsplit", type=int, default=0)
     ap.add_argument("--order", type=int, default=4)
+    ap.add_argument("--path", default="auto",
+                    choices=["auto", "centred", "split"],
+                    help="SPLIT sweeps: the automatic choice, the centred "
+                         "kernels or the double-single split variants")
     a = ap.parse_args(argv)
 
     if a.kernel == "hermite_step":
@@ -50,6 +54,8 @@ def main(argv=None):
     mode = lib.MODE_SPLIT if a.mode == "split" else lib.MODE_EXACT
     if a.variant >= 0:
         lib.set_split_config(a.kernel, a.variant, max(1, a.gsplit))
+    lib.set_centred({"auto": -1, "centred": 1, "split": 0}[a.path], -1,
+                    a.gsplit if a.path == "centred" else 0)
     scal = [1.0 / 64] if a.kernel in ("tstep_kernel", "nreg_Xkernel",
                                       "nreg_Vkernel") else []
     st = torch.cuda.Stream(dev)
@@ -66,12 +72,14 @@ def main(argv=None):
             st.synchronize()
             times.append(e0.elapsed_time(e1) / 1e3)
     lib.check()
-    v, g = lib.split_choice(a.kernel, a.ni, a.nj)
+    path, cfg, g = lib.sweep_plan(a.kernel, a.ni, a.nj)
+    lib.set_centred(-1, -1, 0)
     best = min(times)
     print(json.dumps({"kernel": a.kernel, "mode": a.mode, "ni": a.ni,
                       "nj": a.nj, "times_s": times,
                       "gint_s": a.ni * a.nj / best / 1e9,
-                      "variant": v, "gsplit": g}))
+                      "path": "centred" if path == 1 else "split",
+                      "config": cfg, "gsplit": g}))
 
 
 def hermite_steps(a):
