@@ -50,11 +50,12 @@ def solve(torch, form, dt, m, e2, st, use_mlp=False):
     return out.cpu().numpy(), iters.cpu().numpy()
 
 
-# Softened pairs only at the short step: over long steps the reference's
-# energy check keeps subdividing softened eccentric orbits until the solve
-# budget runs out, which is slow in both the library and the oracle.
-CASES = [(1.0 / 512, False), (1.0 / 32, False), (1.0 / 4, False),
-         (1.0 / 512, True)]
+# Unsoftened pairs: with softening the reference's energy check compares a
+# Keplerian solution against the softened energy and keeps subdividing
+# eccentric orbits until the solve budget runs out (status 3 in every form);
+# softened pairs are covered at the Sakura level, where the reference's
+# leapfrog branch takes them.
+CASES = [(1.0 / 512, False), (1.0 / 32, False), (1.0 / 4, False)]
 
 
 @pytest.mark.parametrize("dt,soft", CASES)
@@ -74,7 +75,10 @@ def test_mixed_form_matches_oracle(dt, soft):
     want, it_w, _ = oracle.kepler_pairs(dt, m, e2, st)
     got, it_g = solve(torch, "mixed", dt, m, e2, st)
     scale = np.abs(st).max(axis=1, keepdims=True)
-    assert np.all(np.abs(got - want) <= 1e-12 * scale)
+    dev = (np.abs(got - want) / scale).max(axis=1)
+    print("dt=%g max %.3g, pairs above 1e-12: %d, worst %s" % (
+        dt, dev.max(), int((dev > 1e-12).sum()), np.argsort(dev)[-3:]))
+    assert np.all(dev <= 1e-12)
     # FP64 updates: the reference form needs at least two per solve (one to
     # move, one to see the update fall below the tolerance)
     assert it_g.mean() < it_w.mean()

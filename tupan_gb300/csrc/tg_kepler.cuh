@@ -379,8 +379,8 @@ __device__ inline int kep_laguerre_f32(float x0, float *x,
 // of 2^-42: the root then lies within that bound of the reference's.
 // S[1..3] receive S1..S3 at the root, shifted from the last evaluation point
 // by their Taylor series in d (dS_{k+1}/ds = S_k, dS_0/ds = al S_1) to
-// second order (d is FP32-small, so the third-order term is below double
-// rounding).
+// second order when |d| <= 2^-20 |s| (the third-order term is then below
+// double rounding), else evaluated at the root.
 __device__ inline int kep_laguerre_mixed(double x0, double *x,
                                          const KepArg<double> &k, int *iters,
                                          int *iters32, double *S)
@@ -407,10 +407,16 @@ __device__ inline int kep_laguerre_mixed(double x0, double *x,
             fabs(delta) <= tol ||
             fabs(ddfv / (2.0 * dfv)) * (delta * delta) <= 0.25 * tol;
         if (done) {
-            const double d = delta, h = 0.5 * delta * delta;
-            S[1] = Sp[1] + d * Sp[0] + h * (k.al * Sp[1]);
-            S[2] = Sp[2] + d * Sp[1] + h * Sp[0];
-            S[3] = Sp[3] + d * Sp[2] + h * Sp[1];
+            if (fabs(delta) <= 9.5367431640625e-7 * fabs(s)) {   // 2^-20 |s|
+                const double d = delta, h = 0.5 * delta * delta;
+                S[1] = Sp[1] + d * Sp[0] + h * (k.al * Sp[1]);
+                S[2] = Sp[2] + d * Sp[1] + h * Sp[0];
+                S[3] = Sp[3] + d * Sp[2] + h * Sp[1];
+            } else {
+                // a large last update (an FP32 stage that did not converge):
+                // the Taylor shift would not be exact enough, evaluate
+                kep_S(s, k.al, S);
+            }
             break;
         }
         if (it > KEPLER_MAXITER) { *iters = it; return -2; }
