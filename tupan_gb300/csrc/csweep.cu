@@ -27,8 +27,9 @@
 //    (FFMA2/FADD2/FMUL2) evaluates one i against two j, and the i operands,
 //    constant over a tile, are duplicated into register pairs once per tile
 //    instead of duplicating every j operand.
-//  * Sums run in FP32 over runs of 16 j per lane half (4 in near tiles),
-//    then fold into a Kahan (sum, correction) pair; the result is formed in
+//  * Sums run in FP32 over runs of 16 j per lane half (4 in near tiles, 32
+//    for the jerk sums of far tiles), then fold into a Kahan (sum,
+//    correction) pair; the result is formed in
 //    double, scattered back to the caller's particle order.  A grid j-split
 //    writes partial sums that a second kernel reduces in a fixed order.
 //  * Tiles reach shared memory by bulk asynchronous copies (cp.async.bulk)
@@ -599,17 +600,20 @@ __global__ void __launch_bounds__(NT, MINB) ct_sweep(const CtLaunch L)
     // N = 3000 with 8 quads everywhere, 6.3e-7 with 2 quads in near tiles,
     // which is the pair arithmetic's own floor there), so near tiles fold
     // every 2 quads.
+    // In far tiles the jerk sums (outputs 3..5 of AccJerk), whose bound is
+    // the loose one, fold every other run: 64 records per fold.
     auto run_tile = [&](const float *F, auto near_tag, auto uni_tag) {
         constexpr bool NEAR = decltype(near_tag)::value;
         constexpr bool UNI = decltype(uni_tag)::value;
         constexpr int RUNQ = NEAR ? 2 : 8;
+        constexpr int NSLOW = (NO == 6 && !NEAR) ? 3 : 0;   // jerk outputs
+        float2 p[NI][NO];
+#pragma unroll
+        for (int k = 0; k < NI; ++k)
+#pragma unroll
+            for (int c = 0; c < NO; ++c) p[k][c] = make_float2(0.f, 0.f);
 #pragma unroll 1
         for (int q0 = 0; q0 < CT; q0 += 4 * RUNQ) {
-            float2 p[NI][NO];
-#pragma unroll
-            for (int k = 0; k < NI; ++k)
-#pragma unroll
-                for (int c = 0; c < NO; ++c) p[k][c] = make_float2(0.f, 0.f);
 #pragma unroll
             for (int u = 0; u < RUNQ; ++u) {
                 const int r = q0 + 4 * u;
@@ -643,11 +647,15 @@ __global__ void __launch_bounds__(NT, MINB) ct_sweep(const CtLaunch L)
                     }
                 }
             }
+            const bool slow = NSLOW > 0 && ((q0 / (4 * RUNQ)) & 1) == 0;
 #pragma unroll
             for (int k = 0; k < NI; ++k)
 #pragma unroll
-                for (int c = 0; c < NO; ++c)
+                for (int c = 0; c < NO; ++c) {
+                    if (c >= NO - NSLOW && slow) continue;
                     kahan_add(sum[k][c], corr[k][c], p[k][c].x + p[k][c].y);
+                    p[k][c] = make_float2(0.f, 0.f);
+                }
         }
     };
 
