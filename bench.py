@@ -138,8 +138,9 @@ def job_rate(interactions_per_rank, world, t_step):
 
 
 def roofline_traffic():
-    """dram bytes per AccJerk launch from the committed ncu summary."""
-    path = os.path.join(ROOT, "profiles", "acc_jerk_split_n262144.md")
+    """dram bytes per AccJerk launch of the bench's kernel from the committed
+    ncu summary (the centred sweep at N = 262144)."""
+    path = os.path.join(ROOT, "profiles", "acc_jerk_centred_n262144.md")
     try:
         for line in open(path):
             if line.startswith("dram_bytes_per_launch:"):

