@@ -150,16 +150,6 @@ def test_centred_matches_split_variants():
         assert e.max() <= 2e-6 and np.median(e) <= 1e-7, name
 
 
-def worst_and_random(ps, n, k, seed):
-    """The k lowest-|a| particles (the Plummer centre, where |a| is a
-    near-cancelling sum) and k random others."""
-    r2 = ps["rx"] ** 2 + ps["ry"] ** 2 + ps["rz"] ** 2
-    low = np.argsort(r2)[:k]
-    rng = np.random.default_rng(seed)
-    rest = np.setdiff1d(np.arange(n), low)
-    return np.sort(np.concatenate([low, rng.choice(rest, k, replace=False)]))
-
-
 @pytest.mark.parametrize("n,k", [(262144, 256), (1048576, 64)])
 def test_centred_configuration_sizes(n, k):
     # Acc and AccJerk of all N against all N (the automatic path at these

