@@ -171,6 +171,10 @@ int tupan_gb300_get_mode(void);
  * reference's retry loops have none. Returns the previous bound. */
 long long tupan_gb300_set_kepler_budget(long long budget);
 
+/* Name of the current CUDA device (NUL-terminated, at most len bytes);
+ * status 1 without a device. */
+int tupan_gb300_device_name(char *buf, int len);
+
 /* SPLIT-mode launch configuration: variant in [0, tupan_gb300_split_variants())
  * and grid j-split count; set_split_config forces it for a kernel
  * (variant < 0 restores the automatic choice), set_tuned records it for sizes
@@ -446,6 +450,16 @@ int tupan_gb300_ensemble_destroy(void *handle);
  * finish in mode 0 (switch_below 0: persistent to the end). */
 int tupan_gb300_ensemble_set_mode(void *handle, int mode, int steps_per_launch,
                                   int switch_below);
+/* Launch shape of the batched sweep: nt threads per CTA (128: four CTAs per
+ * SM; 256: two), ib the i-block of a work item while the active systems fill
+ * the grid (32, 64, 128, 256 or 512; halved and quartered, not below 32, as
+ * systems finish), prefetch 1 to copy the next item's records while the
+ * current one computes.  handle NULL sets the default of ensembles created
+ * later (the autotuner's table sets it on load).  A shape outside these
+ * sets returns status 2 (bad argument). */
+int tupan_gb300_ensemble_set_shape(void *handle, int nt, int ib, int prefetch);
+int tupan_gb300_ensemble_get_shape(void *handle, int *nt, int *ib,
+                                   int *prefetch);
 
 /* ------------------------------------------------------------------------
  * SIA integrators (libtupan_gb300.so only).  No counterpart in the

@@ -120,3 +120,69 @@ def test_ensemble_one_and_two_particle_systems(mode):
             scale = np.abs(ref[c]).max() + 1e-30
             assert np.max(np.abs(st[c][a:b] - ref[c])) <= 1e-6 * scale, (s, c)
     ens.close()
+
+
+# batched sweep launch shapes: (threads per CTA, full i-block, prefetch)
+SHAPES = [(128, 128, 0), (128, 128, 1), (256, 256, 1), (128, 32, 1),
+          (256, 64, 0), (128, 512, 1)]
+
+
+@pytest.mark.parametrize("shape", SHAPES)
+def test_ensemble_shapes_match_per_system_oracle(shape):
+    systems = make_systems(40, lo=3, hi=512, seed=21)
+    t_end, eta = 1.0 / 64, 1.0 / 64
+    ens = DeviceEnsemble(systems, eta)
+    ens.set_shape(*shape)
+    assert ens.shape == shape
+    ens.evolve(t_end, batch=4)
+    t, k, st = ens.state()
+    assert np.all(t == t_end)
+    off = ens.off
+    for s, ps in enumerate(systems):
+        ref = {c: v.copy() for c, v in ps.items()}
+        steps = oi.evolve(ref, t_end, eta, "ahermite4")
+        assert k[s] == len(steps), s
+        a, b = int(off[s]), int(off[s + 1])
+        for c in ("rx", "ry", "rz", "vx", "vy", "vz"):
+            scale = np.abs(ref[c]).max() + 1e-30
+            assert np.max(np.abs(st[c][a:b] - ref[c])) <= 1e-6 * scale, (s, c)
+    ens.close()
+
+
+@pytest.mark.parametrize("nt,ib", [(128, 128), (256, 64)])
+def test_ensemble_prefetch_is_bit_identical(nt, ib):
+    # the double-buffered copy changes when records arrive, not what is
+    # computed from them
+    systems = make_systems(200, lo=3, hi=512, seed=22)
+    out = []
+    for pf in (0, 1):
+        ens = DeviceEnsemble(systems, 1.0 / 64)
+        ens.set_shape(nt, ib, pf)
+        ens.evolve(1.0 / 64, batch=4)
+        out.append(ens.state())
+        ens.close()
+    (t0, k0, s0), (t1, k1, s1) = out
+    np.testing.assert_array_equal(t0, t1)
+    np.testing.assert_array_equal(k0, k1)
+    for c in s0:
+        np.testing.assert_array_equal(s0[c], s1[c])
+
+
+def test_ensemble_shape_default_and_rejects():
+    import tupan_gb300.lib as lib
+    from tupan_gb300 import ensemble as en
+    old = en.default_shape()
+    try:
+        en.set_default_shape(256, 64, 0)
+        systems = make_systems(3, lo=3, hi=30, seed=2)
+        ens = DeviceEnsemble(systems, 1.0 / 64)
+        assert ens.shape == (256, 64, 0)
+        for bad in ((64, 128, 1), (128, 96, 1), (128, 128, 2)):
+            with pytest.raises(lib.TupanGB300Error):
+                ens.set_shape(*bad)
+            with pytest.raises(lib.TupanGB300Error):
+                en.set_default_shape(*bad)
+        ens.evolve(1.0 / 128, batch=2)
+        ens.close()
+    finally:
+        en.set_default_shape(*old)

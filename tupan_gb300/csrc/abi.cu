@@ -793,6 +793,23 @@ TG_EXPORT int tupan_gb300_set_split_config(int kernel, int variant, int gsplit)
     return ST_OK;
 }
 
+// Name of the current CUDA device, NUL-terminated and truncated to len
+// bytes (the key of the autotuner's saved table).
+TG_EXPORT int tupan_gb300_device_name(char *buf, int len)
+{
+    if (!buf || len < 1) return ST_BAD_ARGUMENT;
+    buf[0] = 0;
+    int dev = 0;
+    cudaDeviceProp p;
+    if (cudaGetDevice(&dev) != cudaSuccess ||
+        cudaGetDeviceProperties(&p, dev) != cudaSuccess) {
+        cudaGetLastError();
+        return ST_CUDA;
+    }
+    snprintf(buf, (size_t)len, "%s", p.name);
+    return ST_OK;
+}
+
 // Record a tuned configuration for sizes in the same power-of-two buckets.
 TG_EXPORT int tupan_gb300_set_tuned(int kernel, uint64_t ni, uint64_t nj,
                                     int variant, int gsplit)

@@ -27,6 +27,7 @@
 #include <string.h>
 
 #include <algorithm>
+#include <atomic>
 #include <type_traits>
 #include <numeric>
 #include <vector>
@@ -78,12 +79,13 @@ __device__ __forceinline__ double e_block_tstep(double min_ts, double t,
 // The systems still short of t_end, in processing order (largest first),
 // and the batched sweep's work items in the same order: each active system
 // split into i-blocks, (system, ib | ie << 16) per item, so a large system
-// is spread over several CTAs.  The block is 128 i while the active systems
-// outnumber the sweep's CTAs (fewer items, less reloading of j-records),
-// and shrinks to 64 and 32 i as systems finish, so the last few systems
-// still use many SMs.  One CTA: the per-system step start (activity, base
-// step; t_end is read from device memory, so a captured graph replays with
-// the value of the current evolve call), then a stable compaction.
+// is spread over several CTAs.  The block is the shape's full i-block while
+// the active systems outnumber the sweep's CTAs (fewer items, less
+// reloading of j-records), and shrinks to a half and a quarter of it (not
+// below 32 i) as systems finish, so the last few systems still use many
+// SMs.  One CTA: the per-system step start (activity, base step; t_end is
+// read from device memory, so a captured graph replays with the value of
+// the current evolve call), then a stable compaction.
 constexpr int COMPACT_NT = 1024;
 
 __device__ unsigned block_exclusive_scan(unsigned v, unsigned *wsum,
@@ -110,7 +112,7 @@ __device__ unsigned block_exclusive_scan(unsigned v, unsigned *wsum,
 __global__ void __launch_bounds__(COMPACT_NT)
 k_e_begin(SysCtl *c, int *active, const unsigned *order, const uint64_t *off,
           unsigned ns, const double *t_end_p, double eta, unsigned ctas,
-          unsigned *alist, unsigned *acount, uint2 *items, unsigned *icount,
+          unsigned ib_full, unsigned *alist, unsigned *acount, uint2 *items, unsigned *icount,
           unsigned *sys_items, unsigned *queues)
 {
     // the work counters of the step's four sweeps (a kernel write instead
@@ -133,7 +135,9 @@ k_e_begin(SysCtl *c, int *active, const unsigned *order, const uint64_t *off,
     if ((t & 31) == 0) atomicAdd(&n_active, mine);
     __syncthreads();
     const unsigned na = n_active;
-    const unsigned IB = na >= ctas ? 128u : (na >= ctas / 4 ? 64u : 32u);
+    unsigned IB = na >= ctas ? ib_full : (na >= ctas / 4 ? ib_full / 2
+                                                         : ib_full / 4);
+    IB = IB < 32u ? 32u : IB;
     unsigned sbase = 0, ibase = 0;
     for (unsigned c0 = 0; c0 < ns; c0 += COMPACT_NT) {
         const unsigned k = c0 + t;
@@ -274,10 +278,28 @@ __device__ __forceinline__ void correct_one(const EArrays &A, double tau,
 using AccJerkFast = AccJerkSN<false>;
 using TstepFast = TstepSN<false>;
 
-constexpr int BATCH_NT = 128;             // batched sweep: threads per CTA
-constexpr int BATCH_MINB = 4;             // and CTAs per SM
 constexpr int RUN_NT = 256;               // persistent mode: threads per CTA
 constexpr int BATCH_MAXN = 512;           // largest system held in smem
+
+// Launch shape of the batched sweep: threads per CTA (128 with four CTAs per
+// SM, or 256 with two), the i-block of a work item while the active systems
+// fill the grid (halved and quartered, not below 32, as they finish), and
+// whether a CTA copies its next item's records while it computes the
+// current one (two record buffers, 48 KiB of shared memory per CTA).
+struct EShape {
+    int nt = 128;
+    int ib = 128;
+    int prefetch = 1;
+};
+EShape g_ens_default;                     // shape of new ensembles
+
+inline int shape_minb(const EShape &s) { return s.nt == 256 ? 2 : 4; }
+inline bool shape_valid(int nt, int ib, int prefetch)
+{
+    return (nt == 128 || nt == 256) &&
+           (ib == 32 || ib == 64 || ib == 128 || ib == 256 || ib == 512) &&
+           (prefetch == 0 || prefetch == 1);
+}
 
 struct BatchLaunch {
     const float4 *rec;        // packed records of all systems
@@ -398,28 +420,54 @@ __device__ __forceinline__ void batched_block(double *const *out, float eta,
     }
 }
 
-template <class Op>
-__global__ void __launch_bounds__(BATCH_NT, BATCH_MINB)
+// Validates work item w and, when it is one, starts the bulk copy of its
+// system's records into dst (thread 0 only).  An invalid item is left for
+// the loop, which reports it.
+template <int NF>
+__device__ __forceinline__ bool e_issue(const BatchLaunch &L, unsigned w,
+                                        unsigned n_items, float4 *dst,
+                                        uint64_t *bar)
+{
+    if (w >= n_items) return false;
+    const unsigned sys = L.items[w].x;
+    const uint64_t b = L.off[sys];
+    const int n = (int)(L.off[sys + 1] - b);
+    const int ib = (int)(L.items[w].y & 0xffffu);
+    const int ie = (int)(L.items[w].y >> 16);
+    if (n > BATCH_MAXN || ie > n || ib >= ie) return false;
+    const uint32_t bytes = (uint32_t)(n * NF * sizeof(float4));
+    mbar_arrive_expect_tx(bar, bytes);
+    bulk_g2s(dst, L.rec + b * NF, bytes, bar);
+    return true;
+}
+
+template <class Op, int NT, int MINB, bool PREFETCH>
+__global__ void __launch_bounds__(NT, MINB)
 k_e_sweep(const BatchLaunch L)
 {
     constexpr int NF = Op::NF;
     constexpr bool X2 = !std::is_void<typename X2Of<Op>::type>::value;
-    __shared__ __align__(128) float4 rec[BATCH_MAXN * NF];
-    __shared__ __align__(8) uint64_t bar;
-    __shared__ unsigned item;
+    constexpr int NBUF = PREFETCH ? 2 : 1;
+    constexpr int BUF = BATCH_MAXN * NF;          // float4 per record buffer
+    extern __shared__ __align__(128) float4 e_rec[];
+    __shared__ __align__(8) uint64_t bar[NBUF];
+    __shared__ unsigned item[NBUF];
     __shared__ int last;
     const int tid = threadIdx.x;
+    const unsigned n_items = *L.n_items;
+    // thread 0: buffers with a copy in flight; bit q of phase: the parity
+    // of buffer q's next completion
+    unsigned pending = 0, phase = 0;
     if (tid == 0) {
-        mbar_init(&bar, 1);
+        for (int q = 0; q < NBUF; ++q) mbar_init(&bar[q], 1);
         mbar_init_fence();
+        item[0] = atomicAdd(L.queue, 1u);
+        if (PREFETCH && e_issue<NF>(L, item[0], n_items, e_rec, &bar[0]))
+            pending = 1u;
     }
     __syncthreads();
-    const unsigned n_items = *L.n_items;
-    uint32_t phase = 0;
-    if (tid == 0) item = atomicAdd(L.queue, 1u);
-    __syncthreads();
-    for (;;) {
-        const unsigned w = item;
+    for (int cur = 0;; cur = PREFETCH ? cur ^ 1 : 0) {
+        const unsigned w = item[cur];
         if (w >= n_items) break;
         const unsigned sys = L.items[w].x;
         const uint64_t b = L.off[sys];
@@ -427,28 +475,45 @@ k_e_sweep(const BatchLaunch L)
         const int ib = (int)(L.items[w].y & 0xffffu);
         const int ie = (int)(L.items[w].y >> 16);
         if (n > BATCH_MAXN || ie > n || ib >= ie) {
+            // no copy was started for it; a prefetch is started only after
+            // this check, so none is in flight either
             if (tid == 0) atomicOr(L.err, (unsigned)DERR_BAD_LAUNCH);
             break;
         }
+        float4 *rec = e_rec + cur * BUF;
         if (tid == 0) {
-            const uint32_t bytes = (uint32_t)(n * NF * sizeof(float4));
-            mbar_arrive_expect_tx(&bar, bytes);
-            bulk_g2s(rec, L.rec + b * NF, bytes, &bar);
+            if (PREFETCH) {
+                // the next item's copy runs while this one computes; its
+                // buffer was last read before the previous item's closing
+                // barrier
+                const unsigned nx = atomicAdd(L.queue, 1u);
+                item[cur ^ 1] = nx;
+                if (e_issue<NF>(L, nx, n_items, e_rec + (cur ^ 1) * BUF,
+                                &bar[cur ^ 1]))
+                    pending |= 1u << (cur ^ 1);
+            } else if (e_issue<NF>(L, w, n_items, rec, &bar[0])) {
+                pending |= 1u;
+            }
         }
-        bool got = mbar_wait_bounded(&bar, phase, L.err, L.spin);
+        const bool got = mbar_wait_bounded(&bar[cur], (phase >> cur) & 1u,
+                                           L.err, L.spin);
         if (!__syncthreads_and(got)) {
-            // the copy did not complete in time: wait (bounded) once more
-            // for it before the shared memory goes away, then leave
-            if (tid == 0) mbar_wait_bounded(&bar, phase, L.err);
+            // a copy did not complete in time: wait (bounded) once more for
+            // every copy in flight before the shared memory goes away
+            if (tid == 0)
+                for (int q = 0; q < NBUF; ++q)
+                    if (pending & (1u << q))
+                        mbar_wait_bounded(&bar[q], (phase >> q) & 1u, L.err);
             break;
         }
-        phase ^= 1u;
+        phase ^= 1u << cur;
+        pending &= ~(1u << cur);
         const uint64_t bi = b + ib, ei = b + ie;
         // Tstep sweeps (the one operator with a max output) end in the
         // step size; AccJerk sweeps in the predictor or corrector
         constexpr bool TSTEP_SWEEP = Op::MAXC >= 0;
-        batched_block<Op, X2, BATCH_NT>(L.out, L.eta, L.eta_d, rec, b, n, ib,
-                                        ie - ib);
+        batched_block<Op, X2, NT>(L.out, L.eta, L.eta_d, rec, b, n, ib,
+                                  ie - ib);
         __syncthreads();   // this block's outputs are written (CTA scope)
         if constexpr (TSTEP_SWEEP) {
             if (L.epi == EPI_STEP_SIZE) {
@@ -472,12 +537,12 @@ k_e_sweep(const BatchLaunch L)
             // records go to the buffer the next sweep reads
             const double tau = L.ctl[sys].tau;
             if (L.epi == EPI_PREDICT) {
-                for (uint64_t i = bi + tid; i < ei; i += BATCH_NT) {
+                for (uint64_t i = bi + tid; i < ei; i += NT) {
                     predict_one(L.A, tau, i);
                     e_pack_one(L.A, L.rec_out, i);
                 }
             } else if (L.epi == EPI_CORRECT || L.epi == EPI_CORRECT_END) {
-                for (uint64_t i = bi + tid; i < ei; i += BATCH_NT) {
+                for (uint64_t i = bi + tid; i < ei; i += NT) {
                     correct_one(L.A, tau, i);
                     e_pack_one(L.A, L.rec_out, i);
                 }
@@ -488,11 +553,63 @@ k_e_sweep(const BatchLaunch L)
                 }
             }
         }
-        // every thread read `item` before the copy barrier above, so the
-        // next item can be taken now; the barrier also ends this item's
-        // reads of the shared records before the next copy lands
-        if (tid == 0) item = atomicAdd(L.queue, 1u);
+        // every thread read this item before the copy barrier above; the
+        // closing barrier ends this item's reads of its record buffer
+        // before a copy into it starts
+        if (!PREFETCH && tid == 0) item[0] = atomicAdd(L.queue, 1u);
         __syncthreads();
+    }
+}
+
+template <class Op, int NT, int MINB, bool PREFETCH>
+size_t e_sweep_smem()
+{
+    return (size_t)(PREFETCH ? 2 : 1) * BATCH_MAXN * Op::NF * sizeof(float4);
+}
+
+// Shared-memory limits of every instantiation (above the 48 KiB default for
+// the double-buffered ones); once per process.
+cudaError_t e_sweep_attributes()
+{
+    static std::atomic<int> done{0};
+    if (done.load()) return cudaSuccess;
+    cudaError_t e = cudaSuccess;
+#define TG_E_ATTR(OP, NT, MINB, PF)                                           \
+    if (e == cudaSuccess)                                                     \
+        e = cudaFuncSetAttribute(k_e_sweep<OP, NT, MINB, PF>,                 \
+                                 cudaFuncAttributeMaxDynamicSharedMemorySize, \
+                                 (int)e_sweep_smem<OP, NT, MINB, PF>());
+    TG_E_ATTR(TstepFast, 128, 4, false)
+    TG_E_ATTR(TstepFast, 128, 4, true)
+    TG_E_ATTR(TstepFast, 256, 2, false)
+    TG_E_ATTR(TstepFast, 256, 2, true)
+    TG_E_ATTR(AccJerkFast, 128, 4, false)
+    TG_E_ATTR(AccJerkFast, 128, 4, true)
+    TG_E_ATTR(AccJerkFast, 256, 2, false)
+    TG_E_ATTR(AccJerkFast, 256, 2, true)
+#undef TG_E_ATTR
+    if (e == cudaSuccess) done.store(1);
+    return e;
+}
+
+template <class Op>
+void e_launch(const EShape &sh, unsigned grid, cudaStream_t st,
+              const BatchLaunch &L)
+{
+    if (sh.nt == 256) {
+        if (sh.prefetch)
+            k_e_sweep<Op, 256, 2, true><<<grid, 256,
+                e_sweep_smem<Op, 256, 2, true>(), st>>>(L);
+        else
+            k_e_sweep<Op, 256, 2, false><<<grid, 256,
+                e_sweep_smem<Op, 256, 2, false>(), st>>>(L);
+    } else {
+        if (sh.prefetch)
+            k_e_sweep<Op, 128, 4, true><<<grid, 128,
+                e_sweep_smem<Op, 128, 4, true>(), st>>>(L);
+        else
+            k_e_sweep<Op, 128, 4, false><<<grid, 128,
+                e_sweep_smem<Op, 128, 4, false>(), st>>>(L);
     }
 }
 
@@ -668,6 +785,7 @@ struct Ensemble {
     int mode = 0;                   // 0 batched steps, 1 persistent systems
     int steps_per_launch = 1024;    // persistent: cap per system and launch
     unsigned switch_below = 0;      // persistent -> batched below this many
+    EShape shape;                   // batched sweep launch shape
 };
 
 // One force evaluation of every active system from the current records,
@@ -695,12 +813,12 @@ cudaError_t e_sweep(Ensemble *E, int kernel, double *const *out, double eta,
     L.rec_out = E->pack + (size_t)write_buf * E->n * 3;
     // persistent CTAs; a system of up to 512 particles is at most 16 items
     const uint64_t max_items = (uint64_t)E->ns * 16;
-    const uint64_t ctas = (uint64_t)E->sms * BATCH_MINB;
+    const uint64_t ctas = (uint64_t)E->sms * shape_minb(E->shape);
     const unsigned grid = (unsigned)(ctas < max_items ? ctas : max_items);
     if (kernel == K_TSTEP)
-        k_e_sweep<TstepFast><<<grid, BATCH_NT, 0, E->stream>>>(L);
+        e_launch<TstepFast>(E->shape, grid, E->stream, L);
     else
-        k_e_sweep<AccJerkFast><<<grid, BATCH_NT, 0, E->stream>>>(L);
+        e_launch<AccJerkFast>(E->shape, grid, E->stream, L);
     g_launch_count += 1;
     return cudaGetLastError();
 }
@@ -716,7 +834,8 @@ cudaError_t e_step(Ensemble *E)
     cudaStream_t st = E->stream;
     k_e_begin<<<1, COMPACT_NT, 0, st>>>(E->ctl, E->active, E->order, E->off,
                                         E->ns, E->d_tend, E->eta,
-                                        (unsigned)E->sms * BATCH_MINB, E->alist,
+                                        (unsigned)(E->sms * shape_minb(E->shape)),
+                                        (unsigned)E->shape.ib, E->alist,
                                         E->acount, E->items, E->icount,
                                         E->sys_items, E->queue);
     g_launch_count += 1;
@@ -758,6 +877,8 @@ TG_EXPORT int tupan_gb300_ensemble_create(unsigned n_sys,
     E->n = n;
     E->ns = n_sys;
     E->eta = eta;
+    E->shape = g_ens_default;
+    if (e_sweep_attributes() != cudaSuccess) return ST_CUDA;
     int dev = 0;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&E->sms, cudaDevAttrMultiProcessorCount, dev);
@@ -948,6 +1069,44 @@ TG_EXPORT int tupan_gb300_ensemble_evolve(void *handle, double t_end, int batch,
     unsigned h = 0;
     cudaMemcpy(&h, E->err, sizeof(unsigned), cudaMemcpyDeviceToHost);
     return h ? ST_DEVICE : ST_OK;
+}
+
+// Launch shape of the batched sweep (threads per CTA 128 or 256, full
+// i-block 32..512, prefetch 0/1) of one ensemble, or with handle NULL the
+// default of ensembles created later.  A captured step graph is rebuilt.
+TG_EXPORT int tupan_gb300_ensemble_set_shape(void *handle, int nt, int ib,
+                                             int prefetch)
+{
+    if (!shape_valid(nt, ib, prefetch)) return ST_BAD_ARGUMENT;
+    EShape sh;
+    sh.nt = nt;
+    sh.ib = ib;
+    sh.prefetch = prefetch;
+    Ensemble *E = (Ensemble *)handle;
+    if (!E) {
+        g_ens_default = sh;
+        return ST_OK;
+    }
+    if (cudaStreamSynchronize(E->stream) != cudaSuccess) return ST_CUDA;
+    E->shape = sh;
+    if (E->graph) {
+        cudaGraphExecDestroy(E->graph);
+        E->graph = nullptr;
+        E->graph_batch = -1;
+    }
+    return ST_OK;
+}
+
+// The shape an ensemble (or, handle NULL, a new one) uses.
+TG_EXPORT int tupan_gb300_ensemble_get_shape(void *handle, int *nt, int *ib,
+                                             int *prefetch)
+{
+    const Ensemble *E = (const Ensemble *)handle;
+    const EShape &sh = E ? E->shape : g_ens_default;
+    if (nt) *nt = sh.nt;
+    if (ib) *ib = sh.ib;
+    if (prefetch) *prefetch = sh.prefetch;
+    return ST_OK;
 }
 
 // mode 0: every step of every system in batched launches; mode 1: one CTA

@@ -32,6 +32,28 @@ def _declare(L):
     L.tupan_gb300_ensemble_set_mode.argtypes = [c.c_void_p, c.c_int, c.c_int,
                                                 c.c_int]
     L.tupan_gb300_ensemble_set_mode.restype = c.c_int
+    L.tupan_gb300_ensemble_set_shape.argtypes = [c.c_void_p, c.c_int, c.c_int,
+                                                 c.c_int]
+    L.tupan_gb300_ensemble_set_shape.restype = c.c_int
+    L.tupan_gb300_ensemble_get_shape.argtypes = [c.c_void_p] + [
+        c.POINTER(c.c_int)] * 3
+    L.tupan_gb300_ensemble_get_shape.restype = c.c_int
+
+
+def set_default_shape(nt, ib, prefetch):
+    """Launch shape of ensembles created later (see DeviceEnsemble.set_shape)."""
+    L = lib.load("float64")
+    _declare(L)
+    if L.tupan_gb300_ensemble_set_shape(None, int(nt), int(ib), int(prefetch)):
+        raise lib.TupanGB300Error("bad ensemble shape %r" % ((nt, ib, prefetch),))
+
+
+def default_shape():
+    L = lib.load("float64")
+    _declare(L)
+    v = [ctypes.c_int() for _ in range(3)]
+    L.tupan_gb300_ensemble_get_shape(None, *[ctypes.byref(x) for x in v])
+    return tuple(x.value for x in v)
 
 
 def make_systems(count, lo=3, hi=512, eps=1e-4, seed=1):
@@ -73,6 +95,23 @@ class DeviceEnsemble(object):
         if st:
             raise lib.TupanGB300Error("ensemble_set_mode failed: status %d"
                                       % st)
+
+    def set_shape(self, nt, ib, prefetch=1):
+        """Batched sweep launch shape: nt threads per CTA (128 or 256), ib
+        the full i-block of a work item (32..512), prefetch 1 to overlap the
+        next item's record copy with the current item."""
+        st = self.L.tupan_gb300_ensemble_set_shape(self.h, int(nt), int(ib),
+                                                   int(prefetch))
+        if st:
+            raise lib.TupanGB300Error("ensemble_set_shape failed: status %d"
+                                      % st)
+
+    @property
+    def shape(self):
+        v = [ctypes.c_int() for _ in range(3)]
+        self.L.tupan_gb300_ensemble_get_shape(self.h,
+                                              *[ctypes.byref(x) for x in v])
+        return tuple(x.value for x in v)
 
     def evolve(self, t_end, batch=8):
         mx = ctypes.c_longlong()

@@ -26,12 +26,18 @@ def main(argv=None):
                     choices=["batched", "persistent"])
     ap.add_argument("--steps-per-launch", type=int, default=1024)
     ap.add_argument("--switch-below", type=int, default=0)
+    ap.add_argument("--shape", default="",
+                    help="batched sweep shape nt,ib,prefetch (default: the "
+                         "library's, tuned where a table is saved)")
     a = ap.parse_args(argv)
     from .ensemble import DeviceEnsemble, make_systems
     t0 = time.perf_counter()
     systems = make_systems(a.systems, seed=1)
     ens = DeviceEnsemble(systems, a.eta)
     ens.set_mode(a.mode, a.steps_per_launch, a.switch_below)
+    if a.shape:
+        ens.set_shape(*[int(x) for x in a.shape.split(",")])
+    shape = ens.shape
     ke0, pe0 = ens.energies()
     t1 = time.perf_counter()
     mx = ens.evolve(a.t_end, batch=a.batch)
@@ -43,7 +49,7 @@ def main(argv=None):
     print(json.dumps({
         "systems": a.systems, "particles": int(ens.n), "t_end": a.t_end,
         "mode": a.mode, "steps_per_launch": a.steps_per_launch,
-        "switch_below": a.switch_below,
+        "switch_below": a.switch_below, "shape": list(shape),
         "wall_s": t2 - t1, "setup_s": t1 - t0,
         "systems_per_s": a.systems / (t2 - t1),
         "max_steps": int(mx), "mean_steps": float(k.mean()),

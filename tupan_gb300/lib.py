@@ -76,6 +76,8 @@ def _declare(L):
     L.tupan_gb300_sweep_plan.restype = c.c_int
     L.tupan_gb300_set_pipe_spin_limit.argtypes = [c.c_uint]
     L.tupan_gb300_set_pipe_spin_limit.restype = c.c_uint
+    L.tupan_gb300_device_name.argtypes = [c.c_char_p, c.c_int]
+    L.tupan_gb300_device_name.restype = c.c_int
 
 
 def load(prec="float64"):
@@ -91,7 +93,32 @@ def load(prec="float64"):
             L = ctypes.CDLL(path)
             _declare(L)
             _libs[prec] = L
-        return _libs[prec]
+            fresh = prec == "float64"
+        else:
+            fresh = False
+    if fresh:
+        _apply_tuning()
+    return _libs[prec]
+
+
+def _apply_tuning():
+    """This GPU's saved autotuner entries (split sweep and block-step level
+    shapes, the ensemble shape), once per process; TUPAN_GB300_NO_TUNING=1
+    keeps the built-in choices."""
+    if os.environ.get("TUPAN_GB300_NO_TUNING"):
+        return
+    if device_name() is None:
+        return
+    from . import autotune
+    autotune.apply_saved()
+
+
+def device_name():
+    """Name of the current CUDA device, or None without one."""
+    buf = ctypes.create_string_buffer(256)
+    if load("float64").tupan_gb300_device_name(buf, 256):
+        return None
+    return buf.value.decode()
 
 
 def check(prec="float64"):
