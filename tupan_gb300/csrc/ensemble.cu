@@ -285,11 +285,16 @@ constexpr int BATCH_MAXN = 512;           // largest system held in smem
 // SM, or 256 with two), the i-block of a work item while the active systems
 // fill the grid (halved and quartered, not below 32, as they finish), and
 // whether a CTA copies its next item's records while it computes the
-// current one (two record buffers, 48 KiB of shared memory per CTA).
+// current one (two record buffers, 48 KiB of shared memory per CTA).  The
+// default is the fastest of the twelve shapes on 4096 systems of 3-512
+// (t_end = 1/64 after 1/512 of warm-up, GB300): 128 threads, i-block 128,
+// no prefetch, 0.621 s; with prefetch 0.644 s; 256 threads 0.70-0.98 s.
+// The copy of a system's records is short next to its item's sweep, so
+// hiding it does not pay for the second buffer's occupancy.
 struct EShape {
     int nt = 128;
     int ib = 128;
-    int prefetch = 1;
+    int prefetch = 0;
 };
 EShape g_ens_default;                     // shape of new ensembles
 
