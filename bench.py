@@ -191,14 +191,43 @@ def cpu_baseline(n, ni, ps, single_ni=None):
                             "sample": "ni=%d x nj=%d (%.1f s)" % (k1, n, dt1)}}
 
 
+def kepler_long_step(long_dt, res, kp, learned, best, dl, n8, bufs):
+    """Solves per second of every root-solve form, plain and learned start,
+    on the Kepler-branch pairs at the long step dl (into long_dt)."""
+    s8m, s8e, s8s, o8, i8 = bufs
+    for form in ("reference", "shared", "mixed"):
+        for mlp in (False, True):
+            if mlp and res.get("solves_per_s_learned") is None:
+                continue
+            if mlp:
+                learned.LearnedStart.load().install()
+            old_form = kp.set_form(form)
+            try:
+                t = best(lambda: kp.kepler_pairs(n8, dl, s8m, s8e, s8s, o8,
+                                                 iters=i8, use_mlp=mlp))
+            finally:
+                kp.set_form(old_form)
+                if mlp:
+                    kp.clear_mlp()
+            tag = ("learned_" if mlp else "") + form
+            long_dt["solves_per_s_%s" % tag] = n8 / t
+            long_dt["mean_fp64_updates_%s" % tag] = float(
+                i8.float().mean().item())
+    if long_dt.get("solves_per_s_learned_mixed"):
+        long_dt["learned_mixed_over_plain_reference"] = (
+            long_dt["solves_per_s_learned_mixed"]
+            / long_dt["solves_per_s_reference"])
+
+
 def kepler_solves(torch, stream):
     """Second half of the metric: universal-Kepler pair solves per second on
     the Kepler-branch pairs of a Sakura sweep (Salpeter Plummer N = 4096,
-    eps = 0, dt = 1/512: the config-5 half step), plain first guess and
-    learned start, and the queued Sakura sweep's pair rate."""
+    eps = 0, dt = 1/512: the config-5 half step; and dt = 1/8), plain first
+    guess and learned start, and the queued Sakura sweep's pair rate."""
     import numpy as np
     from tupan_gb300 import ics, learned
     from tupan_gb300 import kepler as kp
+    from tupan_gb300.lib import TupanGB300Error
     dt = 1.0 / 512
     st, m, e2 = learned.kepler_pair_states(4096, 11, dt, flag=-1)
     n = len(m)
@@ -258,6 +287,21 @@ def kepler_solves(torch, stream):
             res["solves_per_s_learned_mixed"] / res["solves_per_s_reference"])
         res["learned_mixed_over_plain_shared"] = (
             res["solves_per_s_learned_mixed"] / res["solves_per_s_shared"])
+    # a long step: the Kepler-branch pairs of the same sphere at dt = 1/8
+    # (longer arcs, more Laguerre updates), every form, plain and learned
+    dl = 1.0 / 8
+    st8, m8, e28 = learned.kepler_pair_states(4096, 11, dl, flag=-1)
+    n8 = len(m8)
+    s8m, s8e, s8s = T(m8), T(e28), T(st8)
+    o8 = torch.zeros((n8, 6), dtype=torch.float64, device="cuda")
+    i8 = torch.zeros(n8, dtype=torch.int32, device="cuda")
+    long_dt = {"pairs": n8, "dt": dl}
+    try:
+        kepler_long_step(long_dt, res, kp, learned, best, dl, n8,
+                         (s8m, s8e, s8s, o8, i8))
+    except TupanGB300Error as exc:
+        long_dt["error"] = str(exc)
+    res["dt_1_8"] = long_dt
     ps = ics.plummer(4096, eps=0.0, seed=11, masses="salpeter")
     names = ("m", "rx", "ry", "rz", "e2", "vx", "vy", "vz")
     d = {k: T(ps[k]) for k in names}
