@@ -617,6 +617,36 @@ def main():
             "acc_split_gints": n * n / (f0.elapsed_time(f1) / 1e3) / 1e9,
             "acc_jerk_split_gints": n * n / (f1.elapsed_time(f2) / 1e3) / 1e9}
 
+    # --- the centred sweeps without mid tiles (every tile beyond 1.25 R on
+    # the one-operation far difference): faster, less accurate on particles
+    # whose net force is a near-cancelling sum ---------------------------
+    mid_off = None
+    if rank == 0:
+        prev_mid = lib.set_centred_mid(0.0)
+        try:
+            step()
+            f0, f1, f2 = (torch.cuda.Event(enable_timing=True)
+                          for _ in range(3))
+            flush.fill_(0.125)
+            f0.record(stream)
+            lib.dev_sweep("acc_kernel", n, p5, n, p5,
+                          [t.data_ptr() for t in d_acc], mode=lib.MODE_SPLIT,
+                          stream=sh)
+            f1.record(stream)
+            lib.dev_sweep("acc_jerk_kernel", n, p8, n, p8,
+                          [t.data_ptr() for t in d_aj], mode=lib.MODE_SPLIT,
+                          stream=sh)
+            f2.record(stream)
+            torch.cuda.synchronize()
+        finally:
+            lib.set_centred_mid(prev_mid)
+        t_mo = f1.elapsed_time(f2) / 1e3
+        mid_off = {
+            "mid_reach": 0.0, "default_mid_reach": prev_mid,
+            "acc_split_gints": n * n / (f0.elapsed_time(f1) / 1e3) / 1e9,
+            "acc_jerk_split_gints": n * n / t_mo / 1e9,
+            "acc_jerk_tflops": achieved_aj(n, t_mo)}
+
     # --- FP64 EXACT path on an i-subset (linear in ni) ---------------------
     ni64 = min(args.fp64_ni, n)
     step(lib.MODE_EXACT, ni64)     # warm
@@ -654,7 +684,9 @@ def main():
                    "formula": "SMs x 128 lanes x 2 flop x SM clock"}
     except Exception:
         nominal = None
-
+    if mid_off is not None and nominal is not None:
+        mid_off["acc_jerk_frac_nominal"] = (mid_off["acc_jerk_tflops"]
+                                            / nominal["value"])
 
     kepler = kepler_solves(torch, stream) if rank == 0 else None
     noalloc = noalloc_rate(torch, dev, ps, sh) if rank == 0 else None
@@ -692,6 +724,7 @@ def main():
                     "acc_rel_err_vs_fp64": acc_err,
                     "newton_form": newton,
                     "split_variants_path": variants_cmp,
+                    "centred_mid_off": mid_off,
                     "noalloc_acc_jerk": noalloc},
         "roofline": {"bound": "fp32",
                      "kernel": kname,

@@ -197,6 +197,13 @@ void tupan_gb300_split_variant_info(int variant, int *ni_per_thread,
  * thread: 0 = one, 1 = two) and grid j-split gsplit: < 0 / <= 0 automatic.
  * Returns 0 or 2 (bad argument). */
 int tupan_gb300_set_centred(int policy, int shape, int gsplit);
+/* Reach of the centred sweep's mid tiles in tile radii (default 3): tiles
+ * with some i of a warp within that reach (and none within 1.25 R) take the
+ * i's low part in the position difference, one FP32 operation per axis more,
+ * for the accuracy of particles whose net force is a near-cancelling sum; a
+ * reach of at most 1.25 turns mid tiles off.  Returns the previous reach, or
+ * -1 (no change) for a reach below 0, above 64 or not a number. */
+double tupan_gb300_set_centred_mid(double reach);
 /* The path a SPLIT sweep of this size takes: *path 1 = centred (*config =
  * shape), 0 = split variants (*config = variant); *gsplit = grid j-split. */
 int tupan_gb300_sweep_plan(int kernel, uint64_t ni, uint64_t nj, int *path,

@@ -97,3 +97,16 @@ def test_library_load_applies_no_table_without_a_device(monkeypatch):
     if lib.device_name() is not None:
         pytest.skip("a GPU is present")
     assert lib.device_name() is None
+
+
+def test_centred_mid_reach_setter():
+    _lib_or_skip()
+    prev = lib.set_centred_mid(2.0)
+    try:
+        assert lib.set_centred_mid(0.0) == 2.0
+        for bad in (-1.0, 65.0, float("nan")):
+            with pytest.raises(lib.TupanGB300Error):
+                lib.set_centred_mid(bad)
+        assert lib.set_centred_mid(0.0) == 0.0
+    finally:
+        lib.set_centred_mid(prev)

@@ -152,6 +152,20 @@ def test_centred_matches_split_variants():
 
 @pytest.mark.parametrize("n,k", [(262144, 256), (1048576, 64)])
 def test_centred_configuration_sizes(n, k):
+    check_configuration_size(n, k)
+
+
+def test_centred_configuration_size_without_mid_tiles():
+    # the one-operation far difference on every tile beyond 1.25 R: the
+    # same bounds (measured on the centre: 8.6e-6 relative)
+    prev = lib.set_centred_mid(0.0)
+    try:
+        check_configuration_size(262144, 256)
+    finally:
+        lib.set_centred_mid(prev)
+
+
+def check_configuration_size(n, k):
     # Acc and AccJerk of all N against all N (the automatic path at these
     # sizes) against the oracle on k random particles and the k lowest-|a|
     # ones at the sphere's centre, plus momentum balance.
@@ -160,9 +174,10 @@ def test_centred_configuration_sizes(n, k):
     # net force is a near-cancelling sum (N = 262144, seed 2024: r = 0.0046,
     # |a| = 0.0065, 50x below the median) is out of reach of FP32 pair
     # arithmetic at 1e-6 on either SPLIT path (measured on it: 4.6e-6 on the
-    # double-single split variants; FP32 pairs on exact differences summed
-    # in fp64 give 2.0e-6); there the bound is 1e-5 relative and, absolute,
-    # 1e-6 of the median |a| (measured up to 5.4e-7 of it).
+    # double-single split variants, 4.55e-6 centred with mid tiles, 8.6e-6
+    # without; FP32 pairs on exact differences summed in fp64 give 2.0e-6);
+    # there the bound is 1e-5 relative and, absolute, 1e-6 of the median
+    # |a| (measured up to 5.4e-7 of it).
     ps = ics.plummer(n, eps=1e-4, seed=2024)
     assert lib.sweep_plan("acc_jerk_kernel", n, n)[0] == 1
     r2 = ps["rx"] ** 2 + ps["ry"] ** 2 + ps["rz"] ** 2

@@ -79,6 +79,8 @@ namespace tg {
 std::atomic<unsigned long long> g_launch_count{0};
 std::atomic<uint32_t> g_pipe_spin{1u << 20};
 uint32_t pipe_spin_limit() { return g_pipe_spin.load(); }
+std::atomic<float> g_centred_mid{3.0f};
+float centred_mid_reach() { return g_centred_mid.load(); }
 }
 
 using namespace tg;
@@ -834,6 +836,16 @@ TG_EXPORT int tupan_gb300_split_choice(int kernel, uint64_t ni, uint64_t nj,
     if (rc) return rc;
     choose_split(d, kernel, ni, nj, variant, gsplit);
     return ST_OK;
+}
+
+// Reach of the centred sweep's mid tiles in tile radii (default 3; at most
+// 1.25, the near reach, turns them off: every tile beyond 1.25 R takes the
+// one-operation far difference).  Returns the previous reach, or -1 (and
+// changes nothing) for a reach that is negative, above 64 or not a number.
+TG_EXPORT double tupan_gb300_set_centred_mid(double reach)
+{
+    if (!(reach >= 0.0 && reach <= 64.0)) return -1.0;
+    return (double)g_centred_mid.exchange((float)reach);
 }
 
 // Centred SPLIT sweeps (Phi, Acc, AccJerk on Morton-ordered, tile-centred

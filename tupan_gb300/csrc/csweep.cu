@@ -8,30 +8,28 @@
 //    bounding box of the i and j sets; a stable LSD radix sort of our own),
 //    so that 256 consecutive j-particles form a compact tile and 32
 //    consecutive i-particles a compact warp.
-//  * A j-tile stores its particles relative to a centre c (one float on a
-//    common grid per axis): delta_j = x_j - c as a normalised double-single
-//    (dh, dl), formed by ds_sub() from the double-single split of x_j.
-//  * Per (warp, tile) the sweep classifies the tile by the warp's sphere
-//    (centre w on the same grid, radius r_w): near when |c - w| <= 1.25 R
-//    + r_w (R the tile radius), else far.  10 % of (warp, tile) pairs are
-//    near on the N = 262144 Plummer sphere.
-//  * Near tiles form D = x_i - c with the same ds_sub() as the tile, so a
-//    particle seen from itself, or from another at the same position,
-//    gives a difference of exactly zero, and take the double-single
-//    difference (dh_j - Dh) + (dl_j - Dl), the r2 > 0 mask and a Newton
-//    step on rsqrt.
-//  * Far tiles take x_j - x_i = w_j - W_i: ONE FP32 operation per axis
-//    instead of the three of the double-single difference, and no mask (no
-//    pair of a far tile can coincide).  w_j = dh_j + (c - w) is formed once
-//    per warp and tile into shared memory (c - w is exact on the grid), W_i
-//    = x_i - w once per sweep; ct_diff() gives the emulated accuracy.
+//  * A j-tile stores its particles relative to a centre c (one float per
+//    axis): delta_j = x_j - c as a normalised double-single (dh, dl), formed
+//    by ds_sub() from the double-single split of x_j.  Per (i, tile) the
+//    sweep forms D = x_i - c with the same ds_sub() from x_i's split, so a
+//    particle seen from itself, or from another at the same position, gives
+//    a difference of exactly zero.
+//  * Far tiles (every i of the warp farther than 3 R from c, R the tile
+//    radius; the mid reach, 3 R, is settable) take x_j - x_i = dh_j - Dh:
+//    ONE FP32 operation per axis instead of the three of the double-single
+//    difference, and no r2 > 0 mask (no pair of a far tile can coincide).
+//    Mid tiles (some i within 3 R, none within 1.25 R) add the i's low
+//    part: (dh_j - Dh) - Dl, two operations.
+//    Near tiles take the double-single difference (dh_j - Dh) + (dl_j - Dl)
+//    and the mask.  On the N = 262144 Plummer sphere 7.5 % of (warp, tile)
+//    pairs are near and 35 % mid; ct_diff() gives the emulated accuracy.
 //  * The tile is stored field by field (structure of arrays), so one 128-bit
 //    shared-memory load gives a field of four j; each packed FP32 operation
 //    (FFMA2/FADD2/FMUL2) evaluates one i against two j, and the i operands,
 //    constant over a tile, are duplicated into register pairs once per tile
 //    instead of duplicating every j operand.
-//  * Sums run in FP32 over runs of 16 j per lane half (4 in near tiles, 32
-//    for the jerk sums of far tiles), then fold into a Kahan (sum,
+//  * Sums run in FP32 over runs of 32 j per lane half in far tiles (64 for
+//    the jerk sums; 4 in near tiles), then fold into a Kahan (sum,
 //    correction) pair; the result is formed in
 //    double, scattered back to the caller's particle order.  A grid j-split
 //    writes partial sums that a second kernel reduces in a fixed order.
@@ -42,7 +40,6 @@
 #include <stdint.h>
 #include <string.h>
 
-#include <atomic>
 #include <type_traits>
 
 #include "tg_common.cuh"
@@ -54,10 +51,11 @@ namespace tg {
 constexpr int CT = 256;           // j-records per tile
 constexpr int CT_HDR = 8;         // header floats in front of a tile's fields
 constexpr int CT_STAGES = 3;      // shared-memory ring depth
-constexpr float CT_NEAR = 1.25f;  // near: the warp's sphere reaches 1.25 R
+constexpr float CT_NEAR = 1.25f;  // near: some i of the warp within 1.25 R
 
-// Classes of a (warp, tile) pair.
-enum CtClass : int { CT_FAR = 0, CT_NEARBY = 1 };
+// Classes of a (warp, tile) pair, from the i of the warp nearest to the
+// tile's centre.
+enum CtClass : int { CT_FAR = 0, CT_MIDDLE = 1, CT_NEARBY = 2 };
 
 // Fields of a j-record in a tile block (each an array of CT floats).
 enum CtField : int {
@@ -106,33 +104,6 @@ __device__ __forceinline__ uint32_t ord_of(float f)
 __device__ __forceinline__ float float_of_ord(uint32_t o)
 {
     return __uint_as_float((o & 0x80000000u) ? (o & 0x7fffffffu) : ~o);
-}
-
-// Exponent e of the grid 2^e that tile and warp centres are rounded to,
-// from the common bounding box: any multiple of 2^e inside the box (or half
-// a step outside it) is an exact float, and so is the difference of any two
-// of them (at most 2^20 + 1 steps apart), so the sweep forms c_tile - c_warp
-// without rounding.
-__device__ __forceinline__ int ct_grid_exp(const uint32_t *box)
-{
-    float ext = 0.f, amax = 0.f;
-#pragma unroll
-    for (int d = 0; d < 3; ++d) {
-        const float lo = float_of_ord(box[d]), hi = float_of_ord(box[3 + d]);
-        ext = fmaxf(ext, hi - lo);
-        amax = fmaxf(amax, fmaxf(fabsf(lo), fabsf(hi)));
-    }
-    int e1 = 0, e2 = 0;
-    frexpf(ext, &e1);     // ext < 2^e1
-    frexpf(amax, &e2);    // amax < 2^e2
-    int e = max(e1 - 20, e2 - 24);
-    return (isfinite(ext) && isfinite(amax)) ? max(e, -100) : 0;
-}
-
-// v rounded to the nearest multiple of 2^e (exact float by ct_grid_exp).
-__device__ __forceinline__ float ct_round_grid(double v, int e)
-{
-    return (float)ldexp(rint(ldexp(v, -e)), e);
 }
 
 // box[0..2]: ordered minima, box[3..5]: ordered maxima (initialised to
@@ -344,8 +315,7 @@ struct CtAttrs {
 // zero to every Phi / Acc / AccJerk sum.
 template <int K>
 __global__ void __launch_bounds__(CT)
-ct_tiles(const CtAttrs A, uint64_t nj, const uint32_t *perm,
-         const uint32_t *box, float *tiles)
+ct_tiles(const CtAttrs A, uint64_t nj, const uint32_t *perm, float *tiles)
 {
     constexpr int NF = ct_nf(K), TB = ct_block_floats(K);
     __shared__ double red[6][CT / 32];
@@ -379,7 +349,7 @@ ct_tiles(const CtAttrs A, uint64_t nj, const uint32_t *perm,
             l = fmin(l, red[t][q]);
             h = fmax(h, red[3 + t][q]);
         }
-        cen[t] = ct_round_grid(0.5 * l + 0.5 * h, ct_grid_exp(box));
+        cen[t] = (float)(0.5 * l + 0.5 * h);
     }
     __syncthreads();
     float dh[3] = {0.f, 0.f, 0.f}, dl[3] = {0.f, 0.f, 0.f};
@@ -458,7 +428,6 @@ __global__ void ct_pack_i(const CtAttrs A, uint64_t ni, const uint32_t *perm,
 struct CtI {
     float xh[3], xl[3], e2;
     float2 ndh[3], ndl[3], nv[3], h2;
-    float2 nw[3];     // -(x_i - c_warp), high part (far tiles)
 };
 
 // j operands of one pair of records
@@ -469,18 +438,16 @@ struct CtJ {
 __device__ __forceinline__ float2 lo2(float4 a) { return make_float2(a.x, a.y); }
 __device__ __forceinline__ float2 hi2(float4 a) { return make_float2(a.z, a.w); }
 
-// x_j - x_i.  Near tiles: the double-single difference relative to the
-// tile's centre c, (dh_j - Dh) + (dl_j - Dl).  Far tiles: both positions
-// relative to the warp's centre w, w_j - W_i with w_j = dh_j + (c - w)
-// (c - w exact; one rounding per j, formed once per warp and tile into
-// shared memory) and W_i the high part of x_i - w (small: the warp is
-// compact in Morton order).  Taking the far difference relative to c
-// instead, dh_j - Dh, would drop Dl, up to half an ulp of |x_i - c|,
-// shared by every pair of the tile: the tile's pull evaluated at a point
-// shifted by Dl.  On a particle whose net force is a near-cancelling sum
-// that shift dominates.  Emulated in FP32 on the N = 262144 Plummer sphere
-// (the 64 particles nearest its centre, pair terms summed in fp64): max
-// |da|/|a| 6.5e-6 relative to c, 2.75e-6 relative to w, 2.0e-6 with the
+// x_j - x_i.  Near: the double-single difference.  Far: dh_j - Dh, which
+// drops Dl, the low part of D = x_i - c: up to half an ulp of |D| of
+// error shared by every pair of the tile, so the tile's pull on i is
+// evaluated at a point shifted by Dl.  Where the tile is close (mid: within
+// 3 R) that shift is the largest error left on a particle whose net force
+// is a near-cancelling sum, and the difference takes Dl too,
+// (dh_j - Dh) - Dl: one more operation per axis.  Emulated in FP32 on the
+// N = 262144 Plummer sphere (the 64 particles nearest its centre, pair
+// terms summed in fp64): max |da|/|a| 6.5e-6 with the far form everywhere
+// outside 1.25 R, 3.0e-6 with the mid form to 3 R, 2.0e-6 with the
 // double-single difference everywhere; medians 1.4e-7, 1.3e-7, 1.2e-7.
 template <int CLS>
 __device__ __forceinline__ void ct_diff(const CtI &i, const CtJ &j,
@@ -490,8 +457,10 @@ __device__ __forceinline__ void ct_diff(const CtI &i, const CtJ &j,
     for (int a = 0; a < 3; ++a) {
         if constexpr (CLS == CT_NEARBY)
             d[a] = add2(add2(j.dh[a], i.ndh[a]), add2(j.dl[a], i.ndl[a]));
+        else if constexpr (CLS == CT_MIDDLE)
+            d[a] = add2(add2(j.dh[a], i.ndh[a]), i.ndl[a]);
         else
-            d[a] = add2(j.dh[a], i.nw[a]);
+            d[a] = add2(j.dh[a], i.ndh[a]);
     }
 }
 
@@ -587,17 +556,8 @@ struct CtLaunch {
     double *partial;           // gsplit x NO x ni (grid j-split)
     unsigned *err;
     uint32_t spin;             // main-loop wait limit
-    const uint32_t *box;       // common bounding box (centre grid)
+    float mid;                 // mid-tile reach in tile radii
 };
-
-// Shared memory of a sweep CTA: the tile ring, then per warp the far
-// tile's positions relative to the warp's centre (3 x CT floats).
-template <class Op, int NT>
-constexpr size_t ct_smem_bytes()
-{
-    return ((size_t)CT_STAGES * ct_block_floats(Op::K) +
-            (size_t)(NT / 32) * 3 * CT) * sizeof(float);
-}
 
 template <class Op, int NI, int NT, int MINB>
 __global__ void __launch_bounds__(NT, MINB) ct_sweep(const CtLaunch L)
@@ -605,8 +565,7 @@ __global__ void __launch_bounds__(NT, MINB) ct_sweep(const CtLaunch L)
     constexpr int NO = Op::NO, K = Op::K;
     constexpr int TB = ct_block_floats(K);
     static_assert((TB * 4) % 16 == 0, "tile blocks must stay 16-byte aligned");
-    extern __shared__ __align__(128) float ct_smem[];
-    float *ring = ct_smem;
+    __shared__ __align__(128) float ring[CT_STAGES * TB];
     __shared__ __align__(8) uint64_t bar[CT_STAGES];
 
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
@@ -648,45 +607,6 @@ __global__ void __launch_bounds__(NT, MINB) ct_sweep(const CtLaunch L)
             ip[k].nv[2] = dup(-c.z);
         }
     }
-    // the warp's centre w on the tile centres' grid, each i relative to it,
-    // and the warp's radius about w
-    float wc[3];
-    float rw;
-    {
-        const int ge = ct_grid_exp(L.box);
-        float r2 = 0.f;
-#pragma unroll
-        for (int a = 0; a < 3; ++a) {
-            float lo = ip[0].xh[a], hi = ip[0].xh[a];
-#pragma unroll
-            for (int k = 1; k < NI; ++k) {
-                lo = fminf(lo, ip[k].xh[a]);
-                hi = fmaxf(hi, ip[k].xh[a]);
-            }
-#pragma unroll
-            for (int off = 16; off > 0; off >>= 1) {
-                lo = fminf(lo, __shfl_xor_sync(0xffffffffu, lo, off));
-                hi = fmaxf(hi, __shfl_xor_sync(0xffffffffu, hi, off));
-            }
-            wc[a] = ct_round_grid(0.5 * (double)lo + 0.5 * (double)hi, ge);
-        }
-#pragma unroll
-        for (int k = 0; k < NI; ++k) {
-            float dh[3], dl[3];
-#pragma unroll
-            for (int a = 0; a < 3; ++a) {
-                ds_sub(ip[k].xh[a], ip[k].xl[a], wc[a], dh[a], dl[a]);
-                ip[k].nw[a] = dup(-dh[a]);
-            }
-            r2 = fmaxf(r2, fmaf(dh[2], dh[2], fmaf(dh[1], dh[1], dh[0] * dh[0])));
-        }
-#pragma unroll
-        for (int off = 16; off > 0; off >>= 1)
-            r2 = fmaxf(r2, __shfl_xor_sync(0xffffffffu, r2, off));
-        rw = sqrtf(r2) * 1.0001f;
-    }
-    float *Wb = ct_smem + CT_STAGES * TB + warp * 3 * CT;
-
     float sum[NI][NO], corr[NI][NO];
 #pragma unroll
     for (int k = 0; k < NI; ++k)
@@ -702,14 +622,21 @@ __global__ void __launch_bounds__(NT, MINB) ct_sweep(const CtLaunch L)
     // N = 3000 with 8 quads everywhere, 6.3e-7 with 2 quads in near tiles,
     // which is the pair arithmetic's own floor there), so near tiles fold
     // every 2 quads.
-    // In far tiles the jerk sums (outputs 3..5 of AccJerk), whose bound is
-    // the loose one, fold every other run: 64 records per fold.
+    // Far (and mid) tiles fold the Phi/Acc sums every other run (64
+    // records) and the jerk sums (outputs 3..5 of AccJerk, whose bound is
+    // the loose one) every fourth (128): the terms of a far tile are small
+    // next to the running sum.  Emulated with the kernel's order of FP32
+    // runs and Kahan folds (N = 262144 sphere, the 24 particles nearest its
+    // centre and 24 random ones, mid form): max |da|/|a| 3.35e-6 with
+    // 32-record folds, 3.0e-6 with 64; random particles 3.4e-8 and 3.5e-8.
     auto run_tile = [&](const float *F, auto cls_tag, auto uni_tag) {
         constexpr int CLS = decltype(cls_tag)::value;
         constexpr bool NEAR = CLS == CT_NEARBY;
         constexpr bool UNI = decltype(uni_tag)::value;
         constexpr int RUNQ = NEAR ? 2 : 8;
-        constexpr int NSLOW = (NO == 6 && !NEAR) ? 3 : 0;   // jerk outputs
+        constexpr int PA = NEAR ? 1 : 2;     // runs per fold: Phi, Acc sums
+        constexpr int PJ = NEAR ? 1 : 4;     // runs per fold: jerk sums
+        static_assert(CT % (4 * RUNQ * PJ) == 0, "a tile ends on a fold");
         float2 p[NI][NO];
 #pragma unroll
         for (int k = 0; k < NI; ++k)
@@ -724,8 +651,7 @@ __global__ void __launch_bounds__(NT, MINB) ct_sweep(const CtLaunch L)
                 [[maybe_unused]] float4 V[3];
 #pragma unroll
                 for (int a = 0; a < 3; ++a) {
-                    DH[a] = NEAR ? *(const float4 *)(F + (F_DHX + a) * CT + r)
-                                 : *(const float4 *)(Wb + a * CT + r);
+                    DH[a] = *(const float4 *)(F + (F_DHX + a) * CT + r);
                     if constexpr (NEAR)
                         DL[a] = *(const float4 *)(F + (F_DLX + a) * CT + r);
                     if constexpr (Op::VEL)
@@ -751,12 +677,14 @@ __global__ void __launch_bounds__(NT, MINB) ct_sweep(const CtLaunch L)
                     }
                 }
             }
-            const bool slow = NSLOW > 0 && ((q0 / (4 * RUNQ)) & 1) == 0;
+            const int run = q0 / (4 * RUNQ);
+            const bool fold_a = (run + 1) % PA == 0;
+            const bool fold_j = (run + 1) % PJ == 0;
 #pragma unroll
             for (int k = 0; k < NI; ++k)
 #pragma unroll
                 for (int c = 0; c < NO; ++c) {
-                    if (c >= NO - NSLOW && slow) continue;
+                    if (!((NO == 6 && c >= 3) ? fold_j : fold_a)) continue;
                     kahan_add(sum[k][c], corr[k][c], p[k][c].x + p[k][c].y);
                     p[k][c] = make_float2(0.f, 0.f);
                 }
@@ -776,51 +704,40 @@ __global__ void __launch_bounds__(NT, MINB) ct_sweep(const CtLaunch L)
         }
         const float *B = &ring[(t % CT_STAGES) * TB];
         const float c[3] = {B[0], B[1], B[2]};
+        const float Rn = B[3] * CT_NEAR, Rm = B[3] * L.mid;
+        const float lim = fmaxf(Rn * Rn, 1e-30f);
+        const float lim_mid = fmaxf(Rm * Rm, 1e-30f);
         const bool uni = B[5] != 0.f;
-        // c - w is exact (both on the grid); the tile is near when the
-        // warp's sphere reaches 1.25 R of c (a NaN distance is near too)
-        float cw[3];
+        bool near = false, mid = false;
 #pragma unroll
-        for (int a = 0; a < 3; ++a) cw[a] = c[a] - wc[a];
-        const float dc2 = fmaf(cw[2], cw[2], fmaf(cw[1], cw[1], cw[0] * cw[0]));
-        const float reach = fmaf(B[3], CT_NEAR, rw);
-        const bool near = __any_sync(0xffffffffu,
-                                     !(dc2 > reach * reach * 1.0001f));
+        for (int k = 0; k < NI; ++k) {
+            float dh[3], dl[3];
 #pragma unroll
-        for (int k = 0; k < NI; ++k) ip[k].h2 = dup(ip[k].e2 + B[4]);
+            for (int a = 0; a < 3; ++a) {
+                ds_sub(ip[k].xh[a], ip[k].xl[a], c[a], dh[a], dl[a]);
+                ip[k].ndh[a] = dup(-dh[a]);
+                ip[k].ndl[a] = dup(-dl[a]);
+            }
+            const float d2 = fmaf(dh[2], dh[2], fmaf(dh[1], dh[1], dh[0] * dh[0]));
+            near = near || !(d2 > lim);
+            mid = mid || !(d2 > lim_mid);
+            ip[k].h2 = dup(ip[k].e2 + B[4]);
+        }
+        near = __any_sync(0xffffffffu, near);
+        mid = __any_sync(0xffffffffu, mid);
         const float *F = B + CT_HDR;
         using T_ = std::true_type;
         using F_ = std::false_type;
         using CN = std::integral_constant<int, CT_NEARBY>;
+        using CM = std::integral_constant<int, CT_MIDDLE>;
         using CF = std::integral_constant<int, CT_FAR>;
         if (near) {
-#pragma unroll
-            for (int k = 0; k < NI; ++k)
-#pragma unroll
-                for (int a = 0; a < 3; ++a) {
-                    float dh, dl;
-                    ds_sub(ip[k].xh[a], ip[k].xl[a], c[a], dh, dl);
-                    ip[k].ndh[a] = dup(-dh);
-                    ip[k].ndl[a] = dup(-dl);
-                }
             if (uni) run_tile(F, CN{}, T_{});
             else run_tile(F, CN{}, F_{});
+        } else if (mid) {
+            if (uni) run_tile(F, CM{}, T_{});
+            else run_tile(F, CM{}, F_{});
         } else {
-            // the tile's positions relative to w, once for the warp:
-            // each lane takes float4 quads lane and lane + 32 of each axis
-#pragma unroll
-            for (int a = 0; a < 3; ++a)
-#pragma unroll
-                for (int h = 0; h < 2; ++h) {
-                    const int q = 4 * (lane + 32 * h);
-                    float4 v = *(const float4 *)(F + (F_DHX + a) * CT + q);
-                    v.x = __fadd_rn(v.x, cw[a]);
-                    v.y = __fadd_rn(v.y, cw[a]);
-                    v.z = __fadd_rn(v.z, cw[a]);
-                    v.w = __fadd_rn(v.w, cw[a]);
-                    *(float4 *)(Wb + a * CT + q) = v;
-                }
-            __syncwarp();
             if (uni) run_tile(F, CF{}, T_{});
             else run_tile(F, CF{}, F_{});
         }
@@ -951,16 +868,8 @@ template <class Op, int NI, int NT, int MINB>
 static cudaError_t ct_run(const CtLaunch &L, int gsplit, cudaStream_t st)
 {
     const uint64_t gx = (L.ni + (uint64_t)NT * NI - 1) / ((uint64_t)NT * NI);
-    constexpr size_t smem = ct_smem_bytes<Op, NT>();
-    static std::atomic<int> attr{0};
-    if (!attr.load()) {
-        TG_CUDA_TRY(cudaFuncSetAttribute(
-            ct_sweep<Op, NI, NT, MINB>,
-            cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-        attr.store(1);
-    }
-    ct_sweep<Op, NI, NT, MINB><<<dim3((unsigned)gx, (unsigned)gsplit), NT,
-                                 smem, st>>>(L);
+    ct_sweep<Op, NI, NT, MINB><<<dim3((unsigned)gx, (unsigned)gsplit), NT, 0,
+                                 st>>>(L);
     g_launch_count += 1;
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess || gsplit == 1) return e;
@@ -1038,16 +947,13 @@ cudaError_t launch_centred(int k, uint64_t ni, const void *const *ia,
     if (ntiles) {
         switch (k) {
         case K_PHI:
-            ct_tiles<K_PHI><<<(unsigned)ntiles, CT, 0, st>>>(AJ, nj, perm_j, box,
-                                                    tiles);
+            ct_tiles<K_PHI><<<(unsigned)ntiles, CT, 0, st>>>(AJ, nj, perm_j, tiles);
             break;
         case K_ACC:
-            ct_tiles<K_ACC><<<(unsigned)ntiles, CT, 0, st>>>(AJ, nj, perm_j, box,
-                                                    tiles);
+            ct_tiles<K_ACC><<<(unsigned)ntiles, CT, 0, st>>>(AJ, nj, perm_j, tiles);
             break;
         default:
-            ct_tiles<K_ACC_JERK><<<(unsigned)ntiles, CT, 0, st>>>(AJ, nj, perm_j, box,
-                                                    tiles);
+            ct_tiles<K_ACC_JERK><<<(unsigned)ntiles, CT, 0, st>>>(AJ, nj, perm_j, tiles);
             break;
         }
         g_launch_count += 1;
@@ -1072,7 +978,7 @@ cudaError_t launch_centred(int k, uint64_t ni, const void *const *ia,
     L.partial = (double *)(base + Y.partial);
     L.err = err;
     L.spin = pipe_spin_limit();
-    L.box = box;
+    L.mid = centred_mid_reach();
     switch (k * CT_SHAPES + shape) {
     case K_PHI * CT_SHAPES + 0: return ct_run<CtPhi, 1, 256, 2>(L, geff, st);
     case K_PHI * CT_SHAPES + 1: return ct_run<CtPhi, 2, 256, 1>(L, geff, st);

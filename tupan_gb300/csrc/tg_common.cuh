@@ -19,6 +19,8 @@ extern std::atomic<unsigned long long> g_launch_count;
 // Tries a sweep's main-loop pipeline wait makes before it reports
 // DERR_PIPE_TIMEOUT (defined in abi.cu; tupan_gb300_set_pipe_spin_limit).
 uint32_t pipe_spin_limit();
+// Reach of the centred sweep's mid tiles, in tile radii.
+float centred_mid_reach();
 
 // int(log2(min_ts) - 1), the exponent of tupan's power-of-two step
 // (integrator/__init__.py:59-78), as numpy evaluates it with a correctly

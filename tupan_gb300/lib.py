@@ -71,6 +71,8 @@ def _declare(L):
     L.tupan_gb300_real_bits.restype = c.c_int
     L.tupan_gb300_set_centred.argtypes = [c.c_int, c.c_int, c.c_int]
     L.tupan_gb300_set_centred.restype = c.c_int
+    L.tupan_gb300_set_centred_mid.argtypes = [c.c_double]
+    L.tupan_gb300_set_centred_mid.restype = c.c_double
     L.tupan_gb300_sweep_plan.argtypes = [c.c_int, c.c_uint64, c.c_uint64] + [
         c.POINTER(c.c_int)] * 3
     L.tupan_gb300_sweep_plan.restype = c.c_int
@@ -175,6 +177,15 @@ def set_centred(policy=-1, shape=-1, gsplit=0, prec="float64"):
                                             int(gsplit))
     if st:
         raise TupanGB300Error("bad centred config")
+
+
+def set_centred_mid(reach, prec="float64"):
+    """Mid-tile reach of the centred sweeps in tile radii (<= 1.25: none);
+    returns the previous reach."""
+    prev = load(prec).tupan_gb300_set_centred_mid(float(reach))
+    if prev < 0:
+        raise TupanGB300Error("bad mid-tile reach %r" % (reach,))
+    return prev
 
 
 def sweep_plan(kernel, ni, nj):
