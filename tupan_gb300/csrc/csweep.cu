@@ -9,7 +9,8 @@
 //    so that 256 consecutive j-particles form a compact tile and 32
 //    consecutive i-particles a compact warp.
 //  * A j-tile stores its particles relative to a centre c (one float per
-//    axis): delta_j = x_j - c as a normalised double-single (dh, dl), formed
+//    axis, on a grid common to all tile and warp centres): delta_j = x_j - c
+//    as a normalised double-single (dh, dl), formed
 //    by ds_sub() from the double-single split of x_j.  Per (i, tile) the
 //    sweep forms D = x_i - c with the same ds_sub() from x_i's split, so a
 //    particle seen from itself, or from another at the same position, gives
@@ -18,8 +19,9 @@
 //    radius; the mid reach, 3 R, is settable) take x_j - x_i = dh_j - Dh:
 //    ONE FP32 operation per axis instead of the three of the double-single
 //    difference, and no r2 > 0 mask (no pair of a far tile can coincide).
-//    Mid tiles (some i within 3 R, none within 1.25 R) add the i's low
-//    part: (dh_j - Dh) - Dl, two operations.
+//    Mid tiles (some i within 3 R, none within 1.25 R) take both positions
+//    relative to the warp's centre w instead (also one operation per axis;
+//    the tile's positions are shifted to w once per warp and tile).
 //    Near tiles take the double-single difference (dh_j - Dh) + (dl_j - Dl)
 //    and the mask.  On the N = 262144 Plummer sphere 7.5 % of (warp, tile)
 //    pairs are near and 35 % mid; ct_diff() gives the emulated accuracy.
@@ -40,6 +42,7 @@
 #include <stdint.h>
 #include <string.h>
 
+#include <atomic>
 #include <type_traits>
 
 #include "tg_common.cuh"
@@ -104,6 +107,33 @@ __device__ __forceinline__ uint32_t ord_of(float f)
 __device__ __forceinline__ float float_of_ord(uint32_t o)
 {
     return __uint_as_float((o & 0x80000000u) ? (o & 0x7fffffffu) : ~o);
+}
+
+// Exponent e of the grid 2^e that tile and warp centres are rounded to,
+// from the common bounding box: any multiple of 2^e inside the box (or half
+// a step outside it) is an exact float, and so is the difference of any two
+// of them (at most 2^20 + 1 steps apart), so the sweep forms c_tile - c_warp
+// without rounding.
+__device__ __forceinline__ int ct_grid_exp(const uint32_t *box)
+{
+    float ext = 0.f, amax = 0.f;
+#pragma unroll
+    for (int d = 0; d < 3; ++d) {
+        const float lo = float_of_ord(box[d]), hi = float_of_ord(box[3 + d]);
+        ext = fmaxf(ext, hi - lo);
+        amax = fmaxf(amax, fmaxf(fabsf(lo), fabsf(hi)));
+    }
+    int e1 = 0, e2 = 0;
+    frexpf(ext, &e1);     // ext < 2^e1
+    frexpf(amax, &e2);    // amax < 2^e2
+    int e = max(e1 - 20, e2 - 24);
+    return (isfinite(ext) && isfinite(amax)) ? max(e, -100) : 0;
+}
+
+// v rounded to the nearest multiple of 2^e (exact float by ct_grid_exp).
+__device__ __forceinline__ float ct_round_grid(double v, int e)
+{
+    return (float)ldexp(rint(ldexp(v, -e)), e);
 }
 
 // box[0..2]: ordered minima, box[3..5]: ordered maxima (initialised to
@@ -315,7 +345,8 @@ struct CtAttrs {
 // zero to every Phi / Acc / AccJerk sum.
 template <int K>
 __global__ void __launch_bounds__(CT)
-ct_tiles(const CtAttrs A, uint64_t nj, const uint32_t *perm, float *tiles)
+ct_tiles(const CtAttrs A, uint64_t nj, const uint32_t *perm,
+         const uint32_t *box, float *tiles)
 {
     constexpr int NF = ct_nf(K), TB = ct_block_floats(K);
     __shared__ double red[6][CT / 32];
@@ -349,7 +380,7 @@ ct_tiles(const CtAttrs A, uint64_t nj, const uint32_t *perm, float *tiles)
             l = fmin(l, red[t][q]);
             h = fmax(h, red[3 + t][q]);
         }
-        cen[t] = (float)(0.5 * l + 0.5 * h);
+        cen[t] = ct_round_grid(0.5 * l + 0.5 * h, ct_grid_exp(box));
     }
     __syncthreads();
     float dh[3] = {0.f, 0.f, 0.f}, dl[3] = {0.f, 0.f, 0.f};
@@ -427,7 +458,7 @@ __global__ void ct_pack_i(const CtAttrs A, uint64_t ni, const uint32_t *perm,
 // ---------------------------------------------------------------------------
 struct CtI {
     float xh[3], xl[3], e2;
-    float2 ndh[3], ndl[3], nv[3], h2;
+    float2 ndh[3], ndl[3], nv[3], h2;   // -(x_i - c) or, mid, -(x_i - w)
 };
 
 // j operands of one pair of records
@@ -438,17 +469,21 @@ struct CtJ {
 __device__ __forceinline__ float2 lo2(float4 a) { return make_float2(a.x, a.y); }
 __device__ __forceinline__ float2 hi2(float4 a) { return make_float2(a.z, a.w); }
 
-// x_j - x_i.  Near: the double-single difference.  Far: dh_j - Dh, which
-// drops Dl, the low part of D = x_i - c: up to half an ulp of |D| of
-// error shared by every pair of the tile, so the tile's pull on i is
-// evaluated at a point shifted by Dl.  Where the tile is close (mid: within
+// x_j - x_i.  Near tiles: the double-single difference relative to the
+// tile's centre c, (dh_j - Dh) + (dl_j - Dl).  Far tiles: dh_j - Dh, which
+// drops Dl, the low part of D = x_i - c: up to half an ulp of |x_i - c|
+// shared by every pair of the tile, so the tile's pull on i is evaluated
+// at a point shifted by Dl.  Where the tile is close (mid tiles, within
 // 3 R) that shift is the largest error left on a particle whose net force
-// is a near-cancelling sum, and the difference takes Dl too,
-// (dh_j - Dh) - Dl: one more operation per axis.  Emulated in FP32 on the
-// N = 262144 Plummer sphere (the 64 particles nearest its centre, pair
-// terms summed in fp64): max |da|/|a| 6.5e-6 with the far form everywhere
-// outside 1.25 R, 3.0e-6 with the mid form to 3 R, 2.0e-6 with the
-// double-single difference everywhere; medians 1.4e-7, 1.3e-7, 1.2e-7.
+// is a near-cancelling sum, so mid tiles take both positions relative to
+// the warp's centre w instead: w_j - W_i, w_j = dh_j + (c - w) formed once
+// per warp and tile into shared memory (c and w on a common grid, so c - w
+// is exact; one rounding per j), W_i = x_i - w once per sweep (small: the
+// warp is compact in Morton order).  Emulated in FP32 on the N = 262144
+// Plummer sphere (the 64 particles nearest its centre, pair terms summed
+// in fp64): max |da|/|a| 6.5e-6 with the far form everywhere outside
+// 1.25 R, 3.0e-6 with the i's low part added within 3 R, 2.0e-6 with the
+// double-single difference everywhere.
 template <int CLS>
 __device__ __forceinline__ void ct_diff(const CtI &i, const CtJ &j,
                                         float2 *d)
@@ -457,8 +492,6 @@ __device__ __forceinline__ void ct_diff(const CtI &i, const CtJ &j,
     for (int a = 0; a < 3; ++a) {
         if constexpr (CLS == CT_NEARBY)
             d[a] = add2(add2(j.dh[a], i.ndh[a]), add2(j.dl[a], i.ndl[a]));
-        else if constexpr (CLS == CT_MIDDLE)
-            d[a] = add2(add2(j.dh[a], i.ndh[a]), i.ndl[a]);
         else
             d[a] = add2(j.dh[a], i.ndh[a]);
     }
@@ -557,7 +590,17 @@ struct CtLaunch {
     unsigned *err;
     uint32_t spin;             // main-loop wait limit
     float mid;                 // mid-tile reach in tile radii
+    const uint32_t *box;       // common bounding box (centre grid)
 };
+
+// Shared memory of a sweep CTA: the tile ring, then per warp a mid tile's
+// positions relative to the warp's centre (3 x CT floats).
+template <class Op, int NT>
+constexpr size_t ct_smem_bytes()
+{
+    return ((size_t)CT_STAGES * ct_block_floats(Op::K) +
+            (size_t)(NT / 32) * 3 * CT) * sizeof(float);
+}
 
 template <class Op, int NI, int NT, int MINB>
 __global__ void __launch_bounds__(NT, MINB) ct_sweep(const CtLaunch L)
@@ -565,7 +608,8 @@ __global__ void __launch_bounds__(NT, MINB) ct_sweep(const CtLaunch L)
     constexpr int NO = Op::NO, K = Op::K;
     constexpr int TB = ct_block_floats(K);
     static_assert((TB * 4) % 16 == 0, "tile blocks must stay 16-byte aligned");
-    __shared__ __align__(128) float ring[CT_STAGES * TB];
+    extern __shared__ __align__(128) float ct_smem[];
+    float *ring = ct_smem;
     __shared__ __align__(8) uint64_t bar[CT_STAGES];
 
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
@@ -607,6 +651,28 @@ __global__ void __launch_bounds__(NT, MINB) ct_sweep(const CtLaunch L)
             ip[k].nv[2] = dup(-c.z);
         }
     }
+    // the warp's centre w on the tile centres' grid (mid tiles)
+    float wc[3];
+    {
+        const int ge = ct_grid_exp(L.box);
+#pragma unroll
+        for (int a = 0; a < 3; ++a) {
+            float lo = ip[0].xh[a], hi = ip[0].xh[a];
+#pragma unroll
+            for (int k = 1; k < NI; ++k) {
+                lo = fminf(lo, ip[k].xh[a]);
+                hi = fmaxf(hi, ip[k].xh[a]);
+            }
+#pragma unroll
+            for (int off = 16; off > 0; off >>= 1) {
+                lo = fminf(lo, __shfl_xor_sync(0xffffffffu, lo, off));
+                hi = fmaxf(hi, __shfl_xor_sync(0xffffffffu, hi, off));
+            }
+            wc[a] = ct_round_grid(0.5 * (double)lo + 0.5 * (double)hi, ge);
+        }
+    }
+    float *Wb = ct_smem + CT_STAGES * TB + warp * 3 * CT;
+
     float sum[NI][NO], corr[NI][NO];
 #pragma unroll
     for (int k = 0; k < NI; ++k)
@@ -651,7 +717,9 @@ __global__ void __launch_bounds__(NT, MINB) ct_sweep(const CtLaunch L)
                 [[maybe_unused]] float4 V[3];
 #pragma unroll
                 for (int a = 0; a < 3; ++a) {
-                    DH[a] = *(const float4 *)(F + (F_DHX + a) * CT + r);
+                    DH[a] = CLS == CT_MIDDLE
+                                ? *(const float4 *)(Wb + a * CT + r)
+                                : *(const float4 *)(F + (F_DHX + a) * CT + r);
                     if constexpr (NEAR)
                         DL[a] = *(const float4 *)(F + (F_DLX + a) * CT + r);
                     if constexpr (Op::VEL)
@@ -735,6 +803,32 @@ __global__ void __launch_bounds__(NT, MINB) ct_sweep(const CtLaunch L)
             if (uni) run_tile(F, CN{}, T_{});
             else run_tile(F, CN{}, F_{});
         } else if (mid) {
+            // the tile's positions relative to w, once for the warp (c - w
+            // exact on the grid): each lane takes float4 quads lane and
+            // lane + 32 of each axis; each i relative to w
+#pragma unroll
+            for (int k = 0; k < NI; ++k)
+#pragma unroll
+                for (int a = 0; a < 3; ++a) {
+                    float dh, dl;
+                    ds_sub(ip[k].xh[a], ip[k].xl[a], wc[a], dh, dl);
+                    ip[k].ndh[a] = dup(-dh);
+                }
+#pragma unroll
+            for (int a = 0; a < 3; ++a) {
+                const float cwa = c[a] - wc[a];
+#pragma unroll
+                for (int h = 0; h < 2; ++h) {
+                    const int q = 4 * (lane + 32 * h);
+                    float4 v = *(const float4 *)(F + (F_DHX + a) * CT + q);
+                    v.x = __fadd_rn(v.x, cwa);
+                    v.y = __fadd_rn(v.y, cwa);
+                    v.z = __fadd_rn(v.z, cwa);
+                    v.w = __fadd_rn(v.w, cwa);
+                    *(float4 *)(Wb + a * CT + q) = v;
+                }
+            }
+            __syncwarp();
             if (uni) run_tile(F, CM{}, T_{});
             else run_tile(F, CM{}, F_{});
         } else {
@@ -868,8 +962,16 @@ template <class Op, int NI, int NT, int MINB>
 static cudaError_t ct_run(const CtLaunch &L, int gsplit, cudaStream_t st)
 {
     const uint64_t gx = (L.ni + (uint64_t)NT * NI - 1) / ((uint64_t)NT * NI);
-    ct_sweep<Op, NI, NT, MINB><<<dim3((unsigned)gx, (unsigned)gsplit), NT, 0,
-                                 st>>>(L);
+    constexpr size_t smem = ct_smem_bytes<Op, NT>();
+    static std::atomic<int> attr{0};
+    if (!attr.load()) {
+        TG_CUDA_TRY(cudaFuncSetAttribute(
+            ct_sweep<Op, NI, NT, MINB>,
+            cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+        attr.store(1);
+    }
+    ct_sweep<Op, NI, NT, MINB><<<dim3((unsigned)gx, (unsigned)gsplit), NT,
+                                 smem, st>>>(L);
     g_launch_count += 1;
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess || gsplit == 1) return e;
@@ -947,13 +1049,16 @@ cudaError_t launch_centred(int k, uint64_t ni, const void *const *ia,
     if (ntiles) {
         switch (k) {
         case K_PHI:
-            ct_tiles<K_PHI><<<(unsigned)ntiles, CT, 0, st>>>(AJ, nj, perm_j, tiles);
+            ct_tiles<K_PHI><<<(unsigned)ntiles, CT, 0, st>>>(AJ, nj, perm_j, box,
+                                                    tiles);
             break;
         case K_ACC:
-            ct_tiles<K_ACC><<<(unsigned)ntiles, CT, 0, st>>>(AJ, nj, perm_j, tiles);
+            ct_tiles<K_ACC><<<(unsigned)ntiles, CT, 0, st>>>(AJ, nj, perm_j, box,
+                                                    tiles);
             break;
         default:
-            ct_tiles<K_ACC_JERK><<<(unsigned)ntiles, CT, 0, st>>>(AJ, nj, perm_j, tiles);
+            ct_tiles<K_ACC_JERK><<<(unsigned)ntiles, CT, 0, st>>>(AJ, nj, perm_j, box,
+                                                    tiles);
             break;
         }
         g_launch_count += 1;
@@ -979,6 +1084,7 @@ cudaError_t launch_centred(int k, uint64_t ni, const void *const *ia,
     L.err = err;
     L.spin = pipe_spin_limit();
     L.mid = centred_mid_reach();
+    L.box = box;
     switch (k * CT_SHAPES + shape) {
     case K_PHI * CT_SHAPES + 0: return ct_run<CtPhi, 1, 256, 2>(L, geff, st);
     case K_PHI * CT_SHAPES + 1: return ct_run<CtPhi, 2, 256, 1>(L, geff, st);
