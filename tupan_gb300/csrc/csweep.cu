@@ -470,16 +470,16 @@ __device__ __forceinline__ float2 lo2(float4 a) { return make_float2(a.x, a.y); 
 __device__ __forceinline__ float2 hi2(float4 a) { return make_float2(a.z, a.w); }
 
 // x_j - x_i.  Near tiles: the double-single difference relative to the
-// tile's centre c, (dh_j - Dh) + (dl_j - Dl).  Far tiles: dh_j - Dh, which
-// drops Dl, the low part of D = x_i - c: up to half an ulp of |x_i - c|
-// shared by every pair of the tile, so the tile's pull on i is evaluated
-// at a point shifted by Dl.  Where the tile is close (mid tiles, within
-// 3 R) that shift is the largest error left on a particle whose net force
-// is a near-cancelling sum, so mid tiles take both positions relative to
-// the warp's centre w instead: w_j - W_i, w_j = dh_j + (c - w) formed once
-// per warp and tile into shared memory (c and w on a common grid, so c - w
-// is exact; one rounding per j), W_i = x_i - w once per sweep (small: the
-// warp is compact in Morton order).  Emulated in FP32 on the N = 262144
+// tile's centre c, (dh_j - Dh) + (dl_j - Dl).  Far tiles: dh_j - D' with
+// D' = (xh_i - c) + xl_i rounded, within about an ulp of |x_i - c| of the
+// exact D: an error shared by every pair of the tile, so the tile's pull
+// on i is evaluated at a slightly shifted point.  Where the tile is close
+// (mid tiles, within 3 R) that shift is the largest error left on a
+// particle whose net force is a near-cancelling sum, so mid tiles take
+// both positions relative to the warp's centre w instead: w_j - W_i,
+// w_j = dh_j + (c - w) formed once per warp and tile into shared memory
+// (c and w on a common grid, so c - w is exact; one rounding per j),
+// W_i = (xh_i - w) + xl_i (small: the warp is compact in Morton order).  Emulated in FP32 on the N = 262144
 // Plummer sphere (the 64 particles nearest its centre, pair terms summed
 // in fp64): max |da|/|a| 6.5e-6 with the far form everywhere outside
 // 1.25 R, 3.0e-6 with the i's low part added within 3 R, 2.0e-6 with the
@@ -776,15 +776,16 @@ __global__ void __launch_bounds__(NT, MINB) ct_sweep(const CtLaunch L)
         const float lim = fmaxf(Rn * Rn, 1e-30f);
         const float lim_mid = fmaxf(Rm * Rm, 1e-30f);
         const bool uni = B[5] != 0.f;
+        // x_i - c to within an ulp, (xh - c) + xl: the class test and the
+        // far difference; near tiles redo it exactly below
         bool near = false, mid = false;
 #pragma unroll
         for (int k = 0; k < NI; ++k) {
-            float dh[3], dl[3];
+            float dh[3];
 #pragma unroll
             for (int a = 0; a < 3; ++a) {
-                ds_sub(ip[k].xh[a], ip[k].xl[a], c[a], dh[a], dl[a]);
+                dh[a] = __fadd_rn(__fsub_rn(ip[k].xh[a], c[a]), ip[k].xl[a]);
                 ip[k].ndh[a] = dup(-dh[a]);
-                ip[k].ndl[a] = dup(-dl[a]);
             }
             const float d2 = fmaf(dh[2], dh[2], fmaf(dh[1], dh[1], dh[0] * dh[0]));
             near = near || !(d2 > lim);
@@ -800,6 +801,17 @@ __global__ void __launch_bounds__(NT, MINB) ct_sweep(const CtLaunch L)
         using CM = std::integral_constant<int, CT_MIDDLE>;
         using CF = std::integral_constant<int, CT_FAR>;
         if (near) {
+            // D = x_i - c by the tile's own ds_sub(): a particle seen from
+            // itself (or from another at its position) differs by zero
+#pragma unroll
+            for (int k = 0; k < NI; ++k)
+#pragma unroll
+                for (int a = 0; a < 3; ++a) {
+                    float dh, dl;
+                    ds_sub(ip[k].xh[a], ip[k].xl[a], c[a], dh, dl);
+                    ip[k].ndh[a] = dup(-dh);
+                    ip[k].ndl[a] = dup(-dl);
+                }
             if (uni) run_tile(F, CN{}, T_{});
             else run_tile(F, CN{}, F_{});
         } else if (mid) {
@@ -809,11 +821,9 @@ __global__ void __launch_bounds__(NT, MINB) ct_sweep(const CtLaunch L)
 #pragma unroll
             for (int k = 0; k < NI; ++k)
 #pragma unroll
-                for (int a = 0; a < 3; ++a) {
-                    float dh, dl;
-                    ds_sub(ip[k].xh[a], ip[k].xl[a], wc[a], dh, dl);
-                    ip[k].ndh[a] = dup(-dh);
-                }
+                for (int a = 0; a < 3; ++a)
+                    ip[k].ndh[a] = dup(-__fadd_rn(__fsub_rn(ip[k].xh[a], wc[a]),
+                                                  ip[k].xl[a]));
 #pragma unroll
             for (int a = 0; a < 3; ++a) {
                 const float cwa = c[a] - wc[a];
