@@ -264,43 +264,6 @@ __device__ __forceinline__ void correct_one(const EArrays &A, double tau,
     }
 }
 
-// H4.epredict of particle i from its forces f (a, jerk) just reduced, then
-// its records for the next sweep (the arithmetic of predict_one).
-struct EpiPredict {
-    EArrays A;
-    double tau;
-    float4 *rec_out;
-    __device__ void operator()(uint64_t i, const double *f) const
-    {
-        for (int d = 0; d < 3; ++d) {
-            const double a = f[d], j = f[3 + d], v = A.v[d][i];
-            A.r[d][i] = A.r[d][i] + ((j * tau / 3 + a) * tau / 2 + v) * tau;
-            A.v[d][i] = v + (j * tau / 2 + a) * tau;
-        }
-        e_pack_one(A, rec_out, i);
-    }
-};
-
-// H4.ecorrect of particle i from the step's first forces (A.f0) and the
-// forces f just reduced, then its records (the arithmetic of correct_one).
-struct EpiCorrect {
-    EArrays A;
-    double tau;
-    float4 *rec_out;
-    __device__ void operator()(uint64_t i, const double *f) const
-    {
-        for (int d = 0; d < 3; ++d) {
-            const double a0 = A.f0[d][i], a1 = f[d];
-            const double j0 = A.f0[3 + d][i], j1 = f[3 + d];
-            const double v0 = A.v0[d][i], r0 = A.r0[d][i];
-            const double v1 = (((j0 - j1) * tau / 6 + (a0 + a1)) * tau / 2 + v0);
-            A.v[d][i] = v1;
-            A.r[d][i] = (((a0 - a1) * tau / 6 + (v0 + v1)) * tau / 2 + r0);
-        }
-        e_pack_one(A, rec_out, i);
-    }
-};
-
 // ---------------------------------------------------------------------------
 // Batched SPLIT sweep over the (system, i-block) work items of the active
 // systems, one persistent launch per force evaluation.  CTAs take items
@@ -362,22 +325,12 @@ struct BatchLaunch {
     float4 *rec_out;          // records written by the epilogues
 };
 
-// No per-particle stage after the forces.
-struct EpiNone {
-    __device__ void operator()(uint64_t, const double *) const {}
-};
-
 // One system's i-range [ib, ib + ni) against all of its j (records in
-// shared memory); outputs to out[c][b + i].  epi(i, f) then runs particle
-// i's next stage from its finished outputs f, in a lane of the group that
-// reduced them (lane k for the group's k-th particle when the group has
-// that many lanes), so the stage needs no CTA barrier and no re-read of
-// the outputs.
-template <class Op, bool X2, int NT, class Epi = EpiNone>
+// shared memory); outputs to out[c][b + i].
+template <class Op, bool X2, int NT>
 __device__ __forceinline__ void batched_block(double *const *out, float eta,
                                               double eta_d, const float4 *rec,
-                                              uint64_t b, int n, int ib, int ni,
-                                              const Epi &epi = Epi())
+                                              uint64_t b, int n, int ib, int ni)
 {
     constexpr int NF = Op::NF, NO = Op::NO, MAXC = Op::MAXC;
     constexpr int NI = X2 ? 2 : 1;               // i per thread
@@ -463,14 +416,10 @@ __device__ __forceinline__ void batched_block(double *const *out, float eta,
                 }
             }
             const int q = u0 * NI + k;
-            const int owner = lanes >= NI ? k : 0;
-            if (u0 < units && q < ni && (lane == 0 || lane == owner)) {
+            if (lane == 0 && u0 < units && q < ni) {
                 Op::finish(v, eta_d);
-                if (lane == 0) {
 #pragma unroll
-                    for (int c = 0; c < NO; ++c) out[c][b + iv[k]] = v[c];
-                }
-                if (lane == owner) epi(b + iv[k], v);
+                for (int c = 0; c < NO; ++c) out[c][b + iv[k]] = v[c];
             }
         }
     }
@@ -568,10 +517,10 @@ k_e_sweep(const BatchLaunch L)
         // Tstep sweeps (the one operator with a max output) end in the
         // step size; AccJerk sweeps in the predictor or corrector
         constexpr bool TSTEP_SWEEP = Op::MAXC >= 0;
+        batched_block<Op, X2, NT>(L.out, L.eta, L.eta_d, rec, b, n, ib,
+                                  ie - ib);
+        __syncthreads();   // this block's outputs are written (CTA scope)
         if constexpr (TSTEP_SWEEP) {
-            batched_block<Op, X2, NT>(L.out, L.eta, L.eta_d, rec, b, n, ib,
-                                      ie - ib);
-            __syncthreads();   // this block's outputs are written (CTA scope)
             if (L.epi == EPI_STEP_SIZE) {
                 epi_copy(L.A, bi, ei);
                 // publish this item's Tstep outputs, then count it; the
@@ -589,26 +538,24 @@ k_e_sweep(const BatchLaunch L)
                 }
             }
         } else {
-            // the block's predictor or corrector, run per particle by a
-            // lane that holds its reduced forces; records go to the buffer
-            // the next sweep reads
+            // the block's predictor or corrector, spread over the CTA;
+            // records go to the buffer the next sweep reads
             const double tau = L.ctl[sys].tau;
             if (L.epi == EPI_PREDICT) {
-                batched_block<Op, X2, NT>(L.out, L.eta, L.eta_d, rec, b, n,
-                                          ib, ie - ib,
-                                          EpiPredict{L.A, tau, L.rec_out});
+                for (uint64_t i = bi + tid; i < ei; i += NT) {
+                    predict_one(L.A, tau, i);
+                    e_pack_one(L.A, L.rec_out, i);
+                }
             } else if (L.epi == EPI_CORRECT || L.epi == EPI_CORRECT_END) {
-                batched_block<Op, X2, NT>(L.out, L.eta, L.eta_d, rec, b, n,
-                                          ib, ie - ib,
-                                          EpiCorrect{L.A, tau, L.rec_out});
+                for (uint64_t i = bi + tid; i < ei; i += NT) {
+                    correct_one(L.A, tau, i);
+                    e_pack_one(L.A, L.rec_out, i);
+                }
                 // the system's time moves once, by its first item
                 if (L.epi == EPI_CORRECT_END && ib == 0 && tid == 0) {
                     L.ctl[sys].t += tau;
                     L.ctl[sys].nsteps += 1;
                 }
-            } else {
-                batched_block<Op, X2, NT>(L.out, L.eta, L.eta_d, rec, b, n,
-                                          ib, ie - ib);
             }
         }
         // every thread read this item before the copy barrier above; the
