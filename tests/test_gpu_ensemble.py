@@ -186,3 +186,23 @@ def test_ensemble_shape_default_and_rejects():
         ens.close()
     finally:
         en.set_default_shape(*old)
+
+
+@pytest.mark.parametrize("shape", [(128, 128, 0), (256, 64, 1)])
+def test_ensemble_stage_launch_is_bit_identical(shape):
+    # the predictor/corrector as launches of their own or inside the sweeps:
+    # the same arithmetic on the same forces
+    systems = make_systems(150, lo=3, hi=512, seed=23)
+    out = []
+    for split in (0, 1):
+        ens = DeviceEnsemble(systems, 1.0 / 64)
+        ens.set_shape(*shape)
+        ens.set_stage(split)
+        ens.evolve(1.0 / 64, batch=4)
+        out.append(ens.state())
+        ens.close()
+    (t0, k0, s0), (t1, k1, s1) = out
+    np.testing.assert_array_equal(t0, t1)
+    np.testing.assert_array_equal(k0, k1)
+    for c in s0:
+        np.testing.assert_array_equal(s0[c], s1[c])

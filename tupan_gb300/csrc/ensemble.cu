@@ -519,7 +519,8 @@ k_e_sweep(const BatchLaunch L)
         constexpr bool TSTEP_SWEEP = Op::MAXC >= 0;
         batched_block<Op, X2, NT>(L.out, L.eta, L.eta_d, rec, b, n, ib,
                                   ie - ib);
-        __syncthreads();   // this block's outputs are written (CTA scope)
+        // this block's outputs are written (CTA scope), for a stage here
+        if (TSTEP_SWEEP || L.epi != EPI_NONE) __syncthreads();
         if constexpr (TSTEP_SWEEP) {
             if (L.epi == EPI_STEP_SIZE) {
                 epi_copy(L.A, bi, ei);
@@ -615,6 +616,39 @@ void e_launch(const EShape &sh, unsigned grid, cudaStream_t st,
         else
             k_e_sweep<Op, 128, 4, false><<<grid, 128,
                 e_sweep_smem<Op, 128, 4, false>(), st>>>(L);
+    }
+}
+
+// The per-particle stage of an AccJerk sweep as a launch of its own over
+// the same work items (the sweep then runs without it): kind EPI_PREDICT,
+// EPI_CORRECT or EPI_CORRECT_END.  The sweep's warps keep to FP32 work and
+// one barrier less per item; the stage's fp64 loads and stores run
+// coalesced over all SMs.
+__global__ void __launch_bounds__(128)
+k_e_stage(const EArrays A, SysCtl *ctl, const uint64_t *off,
+          const uint2 *items, const unsigned *n_items, float4 *rec_out,
+          int kind)
+{
+    const unsigned n_it = *n_items;
+    for (unsigned w = blockIdx.x; w < n_it; w += gridDim.x) {
+        const unsigned sys = items[w].x;
+        const uint64_t b = off[sys];
+        const int n = (int)(off[sys + 1] - b);
+        const int ib = (int)(items[w].y & 0xffffu);
+        const int ie = (int)(items[w].y >> 16);
+        if (ie > n || ib >= ie) continue;    // the sweep reports it
+        const double tau = ctl[sys].tau;
+        for (int q = ib + (int)threadIdx.x; q < ie; q += (int)blockDim.x) {
+            const uint64_t i = b + (uint64_t)q;
+            if (kind == EPI_PREDICT) predict_one(A, tau, i);
+            else correct_one(A, tau, i);
+            e_pack_one(A, rec_out, i);
+        }
+        // the system's time moves once, by its first item
+        if (kind == EPI_CORRECT_END && ib == 0 && threadIdx.x == 0) {
+            ctl[sys].t += tau;
+            ctl[sys].nsteps += 1;
+        }
     }
 }
 
@@ -791,6 +825,7 @@ struct Ensemble {
     int steps_per_launch = 1024;    // persistent: cap per system and launch
     unsigned switch_below = 0;      // persistent -> batched below this many
     EShape shape;                   // batched sweep launch shape
+    int split_stage = 1;            // AccJerk stages as launches of their own
 };
 
 // One force evaluation of every active system from the current records,
@@ -828,6 +863,21 @@ cudaError_t e_sweep(Ensemble *E, int kernel, double *const *out, double eta,
     return cudaGetLastError();
 }
 
+// The per-particle stage `kind` of the current work items, records to
+// buffer write_buf.
+cudaError_t e_stage(Ensemble *E, int kind, int write_buf)
+{
+    const uint64_t max_items = (uint64_t)E->ns * 16;
+    const uint64_t cap = (uint64_t)E->sms * 8;
+    const unsigned grid = (unsigned)(max_items < cap ? max_items : cap);
+    k_e_stage<<<grid, 128, 0, E->stream>>>(E->A, E->ctl, E->off, E->items,
+                                           E->icount,
+                                           E->pack + (size_t)write_buf * E->n * 3,
+                                           kind);
+    g_launch_count += 1;
+    return cudaGetLastError();
+}
+
 // One Hermite-4 step of every unfinished system (hermite.py:390-410 with
 // epec(2)): the step start and compaction, then four sweeps whose
 // epilogues set the step size, predict, and correct twice.  Records rotate
@@ -845,12 +895,14 @@ cudaError_t e_step(Ensemble *E)
                                         E->sys_items, E->queue);
     g_launch_count += 1;
     cudaError_t e = e_sweep(E, K_TSTEP, E->A.dt, E->eta, EPI_STEP_SIZE, 0, 0, 0);
-    if (e == cudaSuccess)
-        e = e_sweep(E, K_ACC_JERK, E->A.f0, 0.0, EPI_PREDICT, 0, 1, 1);
-    if (e == cudaSuccess)
-        e = e_sweep(E, K_ACC_JERK, E->A.f1, 0.0, EPI_CORRECT, 1, 2, 2);
-    if (e == cudaSuccess)
-        e = e_sweep(E, K_ACC_JERK, E->A.f1, 0.0, EPI_CORRECT_END, 2, 0, 3);
+    const int epis[3] = {EPI_PREDICT, EPI_CORRECT, EPI_CORRECT_END};
+    double *const *outs[3] = {E->A.f0, E->A.f1, E->A.f1};
+    for (int q = 0; q < 3 && e == cudaSuccess; ++q) {
+        const int rb = q, wb = (q + 1) % 3;
+        e = e_sweep(E, K_ACC_JERK, outs[q], 0.0,
+                    E->split_stage ? EPI_NONE : epis[q], rb, wb, q + 1);
+        if (e == cudaSuccess && E->split_stage) e = e_stage(E, epis[q], wb);
+    }
     return e;
 }
 
@@ -1094,6 +1146,24 @@ TG_EXPORT int tupan_gb300_ensemble_set_shape(void *handle, int nt, int ib,
     }
     if (cudaStreamSynchronize(E->stream) != cudaSuccess) return ST_CUDA;
     E->shape = sh;
+    if (E->graph) {
+        cudaGraphExecDestroy(E->graph);
+        E->graph = nullptr;
+        E->graph_batch = -1;
+    }
+    return ST_OK;
+}
+
+// split 1 (default): each AccJerk sweep's per-particle stage (predictor,
+// corrector) runs as a launch of its own after the sweep; 0: inside the
+// sweep, by the CTA that computed each work item.  A captured step graph is
+// rebuilt.
+TG_EXPORT int tupan_gb300_ensemble_set_stage(void *handle, int split)
+{
+    Ensemble *E = (Ensemble *)handle;
+    if (!E || split < 0 || split > 1) return ST_BAD_ARGUMENT;
+    if (cudaStreamSynchronize(E->stream) != cudaSuccess) return ST_CUDA;
+    E->split_stage = split;
     if (E->graph) {
         cudaGraphExecDestroy(E->graph);
         E->graph = nullptr;

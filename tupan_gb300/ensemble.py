@@ -38,6 +38,8 @@ def _declare(L):
     L.tupan_gb300_ensemble_get_shape.argtypes = [c.c_void_p] + [
         c.POINTER(c.c_int)] * 3
     L.tupan_gb300_ensemble_get_shape.restype = c.c_int
+    L.tupan_gb300_ensemble_set_stage.argtypes = [c.c_void_p, c.c_int]
+    L.tupan_gb300_ensemble_set_stage.restype = c.c_int
 
 
 def set_default_shape(nt, ib, prefetch):
@@ -104,6 +106,14 @@ class DeviceEnsemble(object):
                                                    int(prefetch))
         if st:
             raise lib.TupanGB300Error("ensemble_set_shape failed: status %d"
+                                      % st)
+
+    def set_stage(self, split):
+        """1: each AccJerk sweep's predictor/corrector as a launch of its
+        own; 0: inside the sweep (bit-identical results)."""
+        st = self.L.tupan_gb300_ensemble_set_stage(self.h, int(split))
+        if st:
+            raise lib.TupanGB300Error("ensemble_set_stage failed: status %d"
                                       % st)
 
     @property

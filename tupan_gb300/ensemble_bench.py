@@ -29,6 +29,9 @@ def main(argv=None):
     ap.add_argument("--shape", default="",
                     help="batched sweep shape nt,ib,prefetch (default: the "
                          "library's, tuned where a table is saved)")
+    ap.add_argument("--stage", type=int, default=1,
+                    help="1: predictor/corrector as launches of their own; "
+                         "0: inside the sweeps")
     a = ap.parse_args(argv)
     from .ensemble import DeviceEnsemble, make_systems
     t0 = time.perf_counter()
@@ -37,6 +40,7 @@ def main(argv=None):
     ens.set_mode(a.mode, a.steps_per_launch, a.switch_below)
     if a.shape:
         ens.set_shape(*[int(x) for x in a.shape.split(",")])
+    ens.set_stage(a.stage)
     shape = ens.shape
     ke0, pe0 = ens.energies()
     t1 = time.perf_counter()
@@ -50,6 +54,7 @@ def main(argv=None):
         "systems": a.systems, "particles": int(ens.n), "t_end": a.t_end,
         "mode": a.mode, "steps_per_launch": a.steps_per_launch,
         "switch_below": a.switch_below, "shape": list(shape),
+        "stage": a.stage,
         "wall_s": t2 - t1, "setup_s": t1 - t0,
         "systems_per_s": a.systems / (t2 - t1),
         "max_steps": int(mx), "mean_steps": float(k.mean()),
