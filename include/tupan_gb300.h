@@ -467,9 +467,10 @@ int tupan_gb300_ensemble_set_mode(void *handle, int mode, int steps_per_launch,
 int tupan_gb300_ensemble_set_shape(void *handle, int nt, int ib, int prefetch);
 int tupan_gb300_ensemble_get_shape(void *handle, int *nt, int *ib,
                                    int *prefetch);
-/* split 1 (default): the predictor/corrector after each AccJerk sweep runs
- * as a launch of its own over the step's work items; 0: inside the sweep,
- * by the CTA that computed each work item.  Results are bit-identical. */
+/* split 1: the predictor/corrector after each AccJerk sweep runs as a
+ * launch of its own over the step's work items; 0 (default, faster): inside
+ * the sweep, by the CTA that computed each work item.  Results are
+ * bit-identical. */
 int tupan_gb300_ensemble_set_stage(void *handle, int split);
 
 /* ------------------------------------------------------------------------

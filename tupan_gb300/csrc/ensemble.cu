@@ -623,7 +623,8 @@ void e_launch(const EShape &sh, unsigned grid, cudaStream_t st,
 // the same work items (the sweep then runs without it): kind EPI_PREDICT,
 // EPI_CORRECT or EPI_CORRECT_END.  The sweep's warps keep to FP32 work and
 // one barrier less per item; the stage's fp64 loads and stores run
-// coalesced over all SMs.
+// coalesced over all SMs (an option: slower overall, see
+// tupan_gb300_ensemble_set_stage).
 __global__ void __launch_bounds__(128)
 k_e_stage(const EArrays A, SysCtl *ctl, const uint64_t *off,
           const uint2 *items, const unsigned *n_items, float4 *rec_out,
@@ -825,7 +826,7 @@ struct Ensemble {
     int steps_per_launch = 1024;    // persistent: cap per system and launch
     unsigned switch_below = 0;      // persistent -> batched below this many
     EShape shape;                   // batched sweep launch shape
-    int split_stage = 1;            // AccJerk stages as launches of their own
+    int split_stage = 0;            // AccJerk stages as launches of their own
 };
 
 // One force evaluation of every active system from the current records,
@@ -1154,10 +1155,12 @@ TG_EXPORT int tupan_gb300_ensemble_set_shape(void *handle, int nt, int ib,
     return ST_OK;
 }
 
-// split 1 (default): each AccJerk sweep's per-particle stage (predictor,
-// corrector) runs as a launch of its own after the sweep; 0: inside the
-// sweep, by the CTA that computed each work item.  A captured step graph is
-// rebuilt.
+// split 1: each AccJerk sweep's per-particle stage (predictor, corrector)
+// runs as a launch of its own after the sweep; 0 (default): inside the
+// sweep, by the CTA that computed each work item.  Measured on 4096
+// systems to t_end = 1: 50.4 s split, 44.3 s inside (the three extra
+// launches per step and the stage's own pass over the state cost more than
+// the sweep's barrier saves).  A captured step graph is rebuilt.
 TG_EXPORT int tupan_gb300_ensemble_set_stage(void *handle, int split)
 {
     Ensemble *E = (Ensemble *)handle;

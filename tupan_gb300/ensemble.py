@@ -110,7 +110,7 @@ class DeviceEnsemble(object):
 
     def set_stage(self, split):
         """1: each AccJerk sweep's predictor/corrector as a launch of its
-        own; 0: inside the sweep (bit-identical results)."""
+        own; 0 (default, faster): inside the sweep (bit-identical results)."""
         st = self.L.tupan_gb300_ensemble_set_stage(self.h, int(split))
         if st:
             raise lib.TupanGB300Error("ensemble_set_stage failed: status %d"

@@ -29,7 +29,7 @@ def main(argv=None):
     ap.add_argument("--shape", default="",
                     help="batched sweep shape nt,ib,prefetch (default: the "
                          "library's, tuned where a table is saved)")
-    ap.add_argument("--stage", type=int, default=1,
+    ap.add_argument("--stage", type=int, default=0,
                     help="1: predictor/corrector as launches of their own; "
                          "0: inside the sweeps")
     a = ap.parse_args(argv)
