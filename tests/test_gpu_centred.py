@@ -11,10 +11,11 @@ Bounds per particle against the oracle (the reference's fp64 arithmetic):
     on random particles; on the lowest-|a| particles at the sphere's centre
     see test_centred_configuration_sizes;
   * on small spheres: median |da|/|a| <= 1e-7 and max <= 2e-6.  FP32 pair
-    arithmetic reaches about 1.2e-6 on rare particles whose net force is a
-    near-cancelling sum with one close pair several times larger (measured on
-    N = 3000, seed 12: the double-single split path 1.20e-6, the centred
-    path 1.15e-6 on the same particle), so the tight bound is the median;
+    arithmetic reaches about 1.2e-6 to 1.5e-6 on rare particles whose net
+    force is a near-cancelling sum with one close pair several times larger
+    (measured on N = 3000, seed 12: the double-single split path 1.20e-6,
+    the centred path 1.44e-6 on the same particle), so the tight bound is
+    the median;
   * jerk: median <= 1e-6 and max <= 1e-4; phi: max <= 1e-6.
 """
 

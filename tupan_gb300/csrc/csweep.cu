@@ -497,19 +497,18 @@ __device__ __forceinline__ void ct_diff(const CtI &i, const CtJ &j,
     }
 }
 
-// 1/sqrt(s).  Near tiles hold the i's close neighbours, whose pair terms can
-// exceed its net |a| several times (a particle near the centre of a
-// Plummer sphere): there the MUFU approximation is refined by one Newton
-// step, y (3/2 - s y^2 / 2), so that y^3 carries about half the error, and
-// r2 == 0 (self pairs, coincident particles) is masked.  Far tiles take the
-// MUFU value alone (their terms are small next to |a|).
+// 1/sqrt(s): the MUFU approximation alone; near tiles mask r2 == 0 (self
+// pairs, coincident particles).  A Newton step on the near tiles' values
+// (y (3/2 - s y^2 / 2)) measured no better on the worst particles of small
+// spheres (max |da|/|a| 1.16e-6 with it, 1.44e-6 without on N = 3000, seed
+// 12; 6.7e-7 and 9.0e-7 on N = 20000; 9.2e-7 and 7.8e-7 on the 256
+// particles nearest the centre of N = 65536) and cost 0.7 % of the AccJerk
+// sweep.
 template <bool NEAR>
 __device__ __forceinline__ float2 ct_rsq(float2 s, float2 h2)
 {
     float2 y = make_float2(rsqrtf(s.x), rsqrtf(s.y));
     if constexpr (NEAR) {
-        const float2 u = mul2(mul2(s, y), y);
-        y = mul2(y, fma2(u, dup(-0.5f), dup(1.5f)));
         y.x = (s.x > h2.x) ? y.x : 0.0f;
         y.y = (s.y > h2.y) ? y.y : 0.0f;
     }
