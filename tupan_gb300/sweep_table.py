@@ -97,8 +97,11 @@ def main(argv=None):
         rel = np.linalg.norm(ga - wa, axis=0) / np.linalg.norm(wa, axis=0)
         gi_acc = n * n / t_acc / 1e9
         gi_aj = n * n / t_aj / 1e9
+        path, cfg, gsp = lib.sweep_plan("acc_jerk_kernel", n, n)
         print(json.dumps({
             "n": n, "acc_gints": gi_acc, "acc_jerk_gints": gi_aj,
+            "path": "centred" if path == 1 else "split variants",
+            "config": cfg, "gsplit": gsp,
             "acc_frac_fp32": gi_acc * 20 / 1e3 / peak,
             "acc_jerk_frac_fp32": gi_aj * 42 / 1e3 / peak,
             "fp64_exact_acc_jerk_gints": ni * n / t_aj64 / 1e9,
