@@ -103,8 +103,10 @@ int g_centred_shape = -1;
 int g_centred_gsplit = 0;
 // Sweeps of at least this many interactions (and 512 j) take the centred
 // path automatically: below it the sort and tile build cost more than the
-// sweep saves.
-constexpr double CENTRED_MIN_INTERACTIONS = 268435456.0;   // 2^28
+// sweep saves (measured on Plummer spheres, AccJerk / Acc: N = 16384
+// centred 480 / 665 Gint/s against 657 / 1108 on the split variants;
+// N = 65536 centred 943 / 1665 against 860 / 1416).
+constexpr double CENTRED_MIN_INTERACTIONS = 2147483648.0;  // 2^31
 
 struct Tuned {
     int variant, gsplit;
@@ -849,7 +851,7 @@ TG_EXPORT double tupan_gb300_set_centred_mid(double reach)
 }
 
 // Centred SPLIT sweeps (Phi, Acc, AccJerk on Morton-ordered, tile-centred
-// records; csweep.cu): policy -1 automatic (sweeps of at least 2^28
+// records; csweep.cu): policy -1 automatic (sweeps of at least 2^31
 // interactions), 0 never, 1 always; shape < 0 and gsplit <= 0 automatic.
 // Returns ST_OK or ST_BAD_ARGUMENT.
 TG_EXPORT int tupan_gb300_set_centred(int policy, int shape, int gsplit)
