@@ -84,6 +84,27 @@ def test_split_hermite4_energy_and_steps():
     h.close()
 
 
+def test_split_hermite_at_large_n_takes_the_centred_sweeps():
+    # N = 65536: the SPLIT force sweeps of the device driver go through the
+    # centred kernels; two fixed steps agree with the fp64 EXACT run to the
+    # SPLIT force accuracy carried through the steps
+    from tupan_gb300 import lib
+    n = 65536
+    assert lib.sweep_plan("acc_jerk_kernel", n, n)[0] == 1
+    ps = ics.plummer(n, eps=1e-4, seed=5)
+    res = {}
+    for mode in ("split", "exact"):
+        h = DeviceHermite(ps, 1.0 / 256, order=4, adaptive=False, mode=mode)
+        h.evolve(2.0 / 256, batch=2)
+        assert h.nsteps == 2
+        res[mode] = h.state()
+        h.close()
+    for c in ("rx", "ry", "rz", "vx", "vy", "vz"):
+        scale = np.abs(ps[c]).max()
+        dev = np.abs(res["split"][c] - res["exact"][c]).max() / scale
+        assert dev <= 1e-8, (c, dev)
+
+
 # ---------------------------------------------------------------------------
 # Individual block time steps
 # ---------------------------------------------------------------------------
