@@ -10,21 +10,23 @@
 //    consecutive i-particles a compact warp.
 //  * A j-tile stores its particles relative to a centre c (one float per
 //    axis, on a grid common to all tile and warp centres): delta_j = x_j - c
-//    as a normalised double-single (dh, dl), formed
-//    by ds_sub() from the double-single split of x_j.  Per (i, tile) the
-//    sweep forms D = x_i - c with the same ds_sub() from x_i's split, so a
-//    particle seen from itself, or from another at the same position, gives
-//    a difference of exactly zero.
-//  * Far tiles (every i of the warp farther than 3 R from c, R the tile
-//    radius; the mid reach, 3 R, is settable) take x_j - x_i = dh_j - Dh:
-//    ONE FP32 operation per axis instead of the three of the double-single
-//    difference, and no r2 > 0 mask (no pair of a far tile can coincide).
-//    Mid tiles (some i within 3 R, none within 1.25 R) take both positions
-//    relative to the warp's centre w instead (also one operation per axis;
-//    the tile's positions are shifted to w once per warp and tile).
-//    Near tiles take the double-single difference (dh_j - Dh) + (dl_j - Dl)
-//    and the mask.  On the N = 262144 Plummer sphere 7.5 % of (warp, tile)
-//    pairs are near and 35 % mid; ct_diff() gives the emulated accuracy.
+//    as a normalised double-single (dh, dl), formed by ds_sub() from the
+//    double-single split of x_j.
+//  * Per (warp, tile) each i forms D' = (xh_i - c) + xl_i (within an ulp of
+//    x_i - c); the tile is near if some i of the warp lies within 1.25 R of
+//    c (R the tile radius), mid if some i lies within 3 R (the reach is
+//    settable), else far.  On the N = 262144 Plummer sphere 7.5 % of
+//    (warp, tile) pairs are near and 35 % mid.
+//  * Far tiles take x_j - x_i = dh_j - D': ONE FP32 operation per axis
+//    instead of the three of the double-single difference, and no r2 > 0
+//    mask (no pair of a far tile can coincide).  Mid tiles take both
+//    positions relative to the warp's centre w instead (also one operation
+//    per axis; the tile's positions are shifted to w once per warp and
+//    tile).  Near tiles form D = x_i - c with the tile's own ds_sub(), so a
+//    particle seen from itself, or from another at the same position,
+//    differs by exactly zero, and take the double-single difference
+//    (dh_j - Dh) + (dl_j - Dl) and the mask.  ct_diff() gives the emulated
+//    accuracy of each form.
 //  * The tile is stored field by field (structure of arrays), so one 128-bit
 //    shared-memory load gives a field of four j; each packed FP32 operation
 //    (FFMA2/FADD2/FMUL2) evaluates one i against two j, and the i operands,
