@@ -99,3 +99,29 @@ def test_shipped_gate_uses_the_network_where_it_pays():
         assert r["mean_iters_learned"] <= r["mean_iters_plain"] + 0.005
     tail = lambda h: sum(h[5:])
     assert tail(rs[1]["hist_learned"]) < 0.5 * tail(rs[1]["hist_plain"])
+
+
+@pytest.mark.parametrize("bias", [12.0, -12.0])
+def test_bad_network_falls_back_to_the_plain_guess(bias):
+    """A network whose guess is far off (its output bias set to +-12: starts
+    e^12 times too large or too small) costs iterations but never the
+    result: a solve from the learned start that has not converged after
+    KEPLER_LEARNED_MAXITER updates is redone from the plain guess, so the
+    converged states stay those of the plain solver."""
+    pytest.importorskip("torch")
+    from tupan_gb300 import kepler as kp
+    from tupan_gb300.learned import LearnedStart, evaluate
+    net = LearnedStart(seed=3)
+    net.params[-1] = bias
+    net._round()
+    net.gate = float("-inf")
+    net.install()
+    try:
+        r = evaluate(net, 1.0 / 512, seeds=(78,), n_bodies=1024)
+    finally:
+        kp.clear_mlp()
+    print(r)
+    assert r["pairs"] > 0
+    assert r["max_state_diff_rel"] <= 1e-11
+    # the far-off start costs updates before the fallback takes over
+    assert r["mean_iters_learned"] > r["mean_iters_plain"]

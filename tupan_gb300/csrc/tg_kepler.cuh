@@ -28,6 +28,10 @@ template <> struct KeplerTol<float> {
 };
 
 constexpr int KEPLER_MAXITER = 64;
+// Laguerre updates allowed from a learned start before the solve falls back
+// to the plain guess (the plain guess needs at most a handful on the
+// Kepler-branch pairs of a Sakura step: mean 2.0 at dt = 1/512, 2.8 at 1/8).
+constexpr int KEPLER_LEARNED_MAXITER = 8;
 constexpr int KEPLER_MAX_HALVINGS = 40;
 
 template <typename R>
@@ -96,7 +100,8 @@ __device__ __forceinline__ R kep_ddf(R s, const KepArg<R> &k)
 
 // Laguerre iteration of order 5, universal_kepler_solver.h:225-254.
 template <typename R>
-__device__ int kep_laguerre(R x0, R *x, const KepArg<R> &k, int *iters)
+__device__ int kep_laguerre(R x0, R *x, const KepArg<R> &k, int *iters,
+                            int maxit = KEPLER_MAXITER)
 {
     const int ORDER = 5;
     int it = 0;
@@ -115,7 +120,7 @@ __device__ int kep_laguerre(R x0, R *x, const KepArg<R> &k, int *iters)
         delta = -g / h;
         *x += delta;
         it += 1;
-        if (it > KEPLER_MAXITER) { *iters = it; return -2; }
+        if (it > maxit) { *iters = it; return -2; }
     } while (fabs(delta) > KeplerTol<R>::v());
     *iters = it;
     if (sgn(*x) != sgn(x0)) return -3;
@@ -195,6 +200,7 @@ struct KepCtx {
     R start;
     int form = KEP_REFERENCE;
     long long iterations32 = 0;   // FP32 updates (KEP_MIXED)
+    long long fallbacks = 0;      // learned starts redone from the plain guess
 };
 
 // Stumpff c0..c3 of z from one transcendental evaluation: the reference's
@@ -270,7 +276,8 @@ __device__ __forceinline__ bool lag_delta(R fv, R dfv, R ddfv, R *delta)
 
 // kep_laguerre with one S evaluation per update (KEP_SHARED).
 template <typename R>
-__device__ int kep_laguerre_shared(R x0, R *x, const KepArg<R> &k, int *iters)
+__device__ int kep_laguerre_shared(R x0, R *x, const KepArg<R> &k, int *iters,
+                                   int maxit = KEPLER_MAXITER)
 {
     int it = 0;
     R delta;
@@ -282,7 +289,7 @@ __device__ int kep_laguerre_shared(R x0, R *x, const KepArg<R> &k, int *iters)
         if (!lag_delta(fv, dfv, ddfv, &delta)) { *iters = it; return -1; }
         *x += delta;
         it += 1;
-        if (it > KEPLER_MAXITER) { *iters = it; return -2; }
+        if (it > maxit) { *iters = it; return -2; }
     } while (fabs(delta) > KeplerTol<R>::v());
     *iters = it;
     if (sgn(*x) != sgn(x0)) return -3;
@@ -383,7 +390,8 @@ __device__ inline int kep_laguerre_f32(float x0, float *x,
 // double rounding), else evaluated at the root.
 __device__ inline int kep_laguerre_mixed(double x0, double *x,
                                          const KepArg<double> &k, int *iters,
-                                         int *iters32, double *S)
+                                         int *iters32, double *S,
+                                         int maxit = KEPLER_MAXITER)
 {
     const double tol = KeplerTol<double>::v();
     KepArg<float> kf = {(float)k.dt, (float)k.r0, (float)k.rv0, (float)k.m,
@@ -419,7 +427,7 @@ __device__ inline int kep_laguerre_mixed(double x0, double *x,
             }
             break;
         }
-        if (it > KEPLER_MAXITER) { *iters = it; return -2; }
+        if (it > maxit) { *iters = it; return -2; }
     }
     *x = s;
     *iters = it;
@@ -464,51 +472,69 @@ __device__ bool kep_setup(R dt0, R m, R e2, const R *p, KepArg<R> *ka, R *s0)
     return true;
 }
 
-// _universal_kepler_solver, universal_kepler_solver.h:360-463
+// _universal_kepler_solver, universal_kepler_solver.h:360-463.  A learned
+// start gets KEPLER_LEARNED_MAXITER updates; a solve from it that has not
+// converged by then (or fails) is redone from the plain guess, so the plain
+// iteration stays the fallback and judges the network's guess.
 template <typename R>
 __device__ int kep_single(R dt0, R m, R e2, R *p, KepCtx<R> &c)
 {
-    if (c.solves >= c.budget) { c.exhausted = true; return -4; }
-    KepArg<R> ka;
-    R s0;
-    if (!kep_setup(dt0, m, e2, p, &ka, &s0)) return 0;
-    if (c.use_start) {
-        // A learned start must keep the plain guess's sign: the reference
-        // rejects roots whose sign differs from the start (:252).
-        if (sgn(c.start) == sgn(s0) && isfinite(c.start)) s0 = c.start;
-        c.use_start = false;
-    }
-    R s;
-    int it = 0;
-    int err;
-    if constexpr (sizeof(R) == sizeof(double)) {
-        if (c.form == KEP_MIXED) {
-            R S[4];
-            int it32 = 0;
-            err = kep_laguerre_mixed(s0, &s, ka, &it, &it32, S);
+    for (;;) {
+        if (c.solves >= c.budget) { c.exhausted = true; return -4; }
+        KepArg<R> ka;
+        R s0;
+        if (!kep_setup(dt0, m, e2, p, &ka, &s0)) return 0;
+        bool learned = false;
+        if (c.use_start) {
+            // A learned start must keep the plain guess's sign: the
+            // reference rejects roots whose sign differs from the start
+            // (:252).
+            if (sgn(c.start) == sgn(s0) && isfinite(c.start)) {
+                s0 = c.start;
+                learned = true;
+            }
+            c.use_start = false;
+        }
+        const int maxit = learned ? KEPLER_LEARNED_MAXITER : KEPLER_MAXITER;
+        R s;
+        int it = 0;
+        int err;
+        bool done = false;
+        if constexpr (sizeof(R) == sizeof(double)) {
+            if (c.form == KEP_MIXED) {
+                R S[4];
+                int it32 = 0;
+                err = kep_laguerre_mixed(s0, &s, ka, &it, &it32, S, maxit);
+                c.solves += 1;
+                c.iterations += it;
+                c.iterations32 += it32;
+                if (err == 0) kep_update_S(ka.dt, S, ka.r0, m, e2, p);
+                done = true;
+            }
+        }
+        if (!done && c.form == KEP_SHARED) {
+            err = kep_laguerre_shared(s0, &s, ka, &it, maxit);
             c.solves += 1;
             c.iterations += it;
-            c.iterations32 += it32;
-            if (err == 0) kep_update_S(ka.dt, S, ka.r0, m, e2, p);
-            return err;
+            if (err == 0) {
+                R S[4];
+                kep_S(s, ka.al, S);
+                kep_update_S(ka.dt, S, ka.r0, m, e2, p);
+            }
+            done = true;
         }
-    }
-    if (c.form == KEP_SHARED) {
-        err = kep_laguerre_shared(s0, &s, ka, &it);
-        c.solves += 1;
-        c.iterations += it;
-        if (err == 0) {
-            R S[4];
-            kep_S(s, ka.al, S);
-            kep_update_S(ka.dt, S, ka.r0, m, e2, p);
+        if (!done) {
+            err = kep_laguerre(s0, &s, ka, &it, maxit);
+            c.solves += 1;
+            c.iterations += it;
+            if (err == 0) kep_update(ka.dt, s, ka.r0, m, e2, ka.al, p);
+        }
+        if (err != 0 && learned) {
+            c.fallbacks += 1;
+            continue;          // p unchanged; the plain guess takes over
         }
         return err;
     }
-    err = kep_laguerre(s0, &s, ka, &it);
-    c.solves += 1;
-    c.iterations += it;
-    if (err == 0) kep_update(ka.dt, s, ka.r0, m, e2, ka.al, p);
-    return err;
 }
 
 // __universal_kepler_solver, universal_kepler_solver.h:466-507
