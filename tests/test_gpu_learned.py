@@ -105,7 +105,8 @@ def test_shipped_gate_uses_the_network_where_it_pays():
 def test_bad_network_falls_back_to_the_plain_guess(bias):
     """A network whose guess is far off (its output bias set to +-12: starts
     e^12 times too large or too small) costs iterations but never the
-    result: a solve from the learned start that has not converged after
+    result: a start outside the trust region around the plain guess is not
+    taken, and a solve from the learned start that has not converged after
     KEPLER_LEARNED_MAXITER updates is redone from the plain guess, so the
     converged states stay those of the plain solver."""
     pytest.importorskip("torch")
@@ -123,5 +124,5 @@ def test_bad_network_falls_back_to_the_plain_guess(bias):
     print(r)
     assert r["pairs"] > 0
     assert r["max_state_diff_rel"] <= 1e-11
-    # the far-off start costs updates before the fallback takes over
-    assert r["mean_iters_learned"] > r["mean_iters_plain"]
+    # a far-off start never saves updates
+    assert r["mean_iters_learned"] >= r["mean_iters_plain"]

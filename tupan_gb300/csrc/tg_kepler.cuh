@@ -473,7 +473,8 @@ __device__ bool kep_setup(R dt0, R m, R e2, const R *p, KepArg<R> *ka, R *s0)
 }
 
 // _universal_kepler_solver, universal_kepler_solver.h:360-463.  A learned
-// start gets KEPLER_LEARNED_MAXITER updates; a solve from it that has not
+// start is taken only inside a trust region around the plain guess, and
+// gets KEPLER_LEARNED_MAXITER updates; a solve from it that has not
 // converged by then (or fails) is redone from the plain guess, so the plain
 // iteration stays the fallback and judges the network's guess.
 template <typename R>
@@ -486,10 +487,17 @@ __device__ int kep_single(R dt0, R m, R e2, R *p, KepCtx<R> &c)
         if (!kep_setup(dt0, m, e2, p, &ka, &s0)) return 0;
         bool learned = false;
         if (c.use_start) {
-            // A learned start must keep the plain guess's sign: the
-            // reference rejects roots whose sign differs from the start
-            // (:252).
-            if (sgn(c.start) == sgn(s0) && isfinite(c.start)) {
+            // A learned start must keep the plain guess's sign (the
+            // reference rejects roots whose sign differs from the start,
+            // :252) and stay where the Stumpff functions are well scaled:
+            // w = sqrt|al| s (the eccentric or hyperbolic anomaly swept) at
+            // most 4 times the plain guess's or 8 (a bound orbit sweeps
+            // less than 2 pi after the period reduction).  Far beyond, cosh
+            // and sinh reach 1e150 and a cancelling f can pass the stopping
+            // rule at a wrong root.
+            const R sal = sqrt(fabs(ka.al));
+            if (sgn(c.start) == sgn(s0) && isfinite(c.start) &&
+                sal * fabs(c.start) <= fmax(R(4) * sal * fabs(s0), R(8))) {
                 s0 = c.start;
                 learned = true;
             }
