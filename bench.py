@@ -699,6 +699,8 @@ def main():
     achieved = n * n * FLOPS_ACC_JERK / t_aj / 1e12
     traffic = roofline_traffic()
     path_aj, cfg_aj, g_aj = lib.sweep_plan("acc_jerk_kernel", n, n)
+    cur_mid = lib.set_centred_mid(3.0)
+    lib.set_centred_mid(cur_mid)
     kname = ("ct_sweep<CtAccJerk> (centred, shape %d)" % cfg_aj
              if path_aj == 1 else
              "split_sweep<AccJerkS> variant %d" % cfg_aj)
@@ -714,7 +716,8 @@ def main():
                    "l2": "flushed between steps (256 MiB write)",
                    "parallelism": "replicas" if world > 1 else "single GPU",
                    "acc_jerk_path": "centred" if path_aj == 1 else "split",
-                   "acc_jerk_config": cfg_aj, "acc_jerk_gsplit": g_aj},
+                   "acc_jerk_config": cfg_aj, "acc_jerk_gsplit": g_aj,
+                   "centred_mid_reach": cur_mid},
         "kernels": {"acc_split_gints": n * n / t_acc / 1e9,
                     "acc_jerk_split_gints": n * n / t_aj / 1e9,
                     "fp64_exact_gints": fp64_gints,
