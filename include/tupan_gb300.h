@@ -193,8 +193,10 @@ void tupan_gb300_split_variant_info(int variant, int *ni_per_thread,
 /* Centred SPLIT sweeps of phi, acc and acc_jerk: particles in Morton order,
  * j-tiles stored relative to their centre, a one-operation position
  * difference for tiles far from every i of a warp.  policy -1: automatic
- * (sweeps of at least 2^31 interactions), 0: never, 1: always; shape (i per
- * thread: 0 = one, 1 = two) and grid j-split gsplit: < 0 / <= 0 automatic.
+ * (sweeps of at least 2^31 interactions), 0: never, 1: always; shape (0: one
+ * i per thread, 256 threads, two CTAs per SM; 1: two i per thread, one CTA
+ * per SM; 2: one i per thread, 128 threads, four CTAs per SM) and grid
+ * j-split gsplit: < 0 / <= 0 automatic.
  * Returns 0 or 2 (bad argument). */
 int tupan_gb300_set_centred(int policy, int shape, int gsplit);
 /* Reach of the centred sweep's mid tiles in tile radii (default 3): tiles

@@ -69,7 +69,7 @@ def sub(ps, idx):
     return {k: np.ascontiguousarray(v[idx]) for k, v in ps.items()}
 
 
-@pytest.mark.parametrize("shape", [0, 1])
+@pytest.mark.parametrize("shape", [0, 1, 2])
 @pytest.mark.parametrize("n", [1000, 4096, 20000])
 @pytest.mark.parametrize("name", KERNELS)
 def test_centred_accuracy(name, n, shape):

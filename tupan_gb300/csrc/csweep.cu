@@ -936,10 +936,11 @@ size_t centred_workspace_bytes(int k, uint64_t ni, uint64_t nj, bool same,
     return ct_layout(k, ni, nj, same, gsplit).total;
 }
 
-// Launch shapes of the centred sweep: i per thread and CTAs per SM.
-struct CtShape { int ni_per_thread, ctas_per_sm; };
-static const CtShape kCtShapes[] = {{1, 2}, {2, 1}};
-constexpr int CT_SHAPES = 2;
+// Launch shapes of the centred sweep: i per thread, CTAs per SM, threads
+// per CTA.
+struct CtShape { int ni_per_thread, ctas_per_sm, threads; };
+static const CtShape kCtShapes[] = {{1, 2, 256}, {2, 1, 256}, {1, 4, 128}};
+constexpr int CT_SHAPES = 3;
 
 int centred_shape_count() { return CT_SHAPES; }
 
@@ -949,7 +950,7 @@ int centred_choose_gsplit(uint64_t ni, uint64_t nj, int shape, int sms)
 {
     const uint64_t ntiles = (nj + CT - 1) / CT;
     const CtShape S = kCtShapes[shape];
-    const uint64_t ipc = 256ull * S.ni_per_thread;
+    const uint64_t ipc = (uint64_t)S.threads * S.ni_per_thread;
     const uint64_t gx = (ni + ipc - 1) / ipc;
     const double cap = (double)sms * S.ctas_per_sm;
     double best = 1e300;
@@ -1099,11 +1100,15 @@ cudaError_t launch_centred(int k, uint64_t ni, const void *const *ia,
     switch (k * CT_SHAPES + shape) {
     case K_PHI * CT_SHAPES + 0: return ct_run<CtPhi, 1, 256, 2>(L, geff, st);
     case K_PHI * CT_SHAPES + 1: return ct_run<CtPhi, 2, 256, 1>(L, geff, st);
+    case K_PHI * CT_SHAPES + 2: return ct_run<CtPhi, 1, 128, 4>(L, geff, st);
     case K_ACC * CT_SHAPES + 0: return ct_run<CtAcc, 1, 256, 2>(L, geff, st);
     case K_ACC * CT_SHAPES + 1: return ct_run<CtAcc, 2, 256, 1>(L, geff, st);
+    case K_ACC * CT_SHAPES + 2: return ct_run<CtAcc, 1, 128, 4>(L, geff, st);
     case K_ACC_JERK * CT_SHAPES + 0:
         return ct_run<CtAccJerk, 1, 256, 2>(L, geff, st);
-    default: return ct_run<CtAccJerk, 2, 256, 1>(L, geff, st);
+    case K_ACC_JERK * CT_SHAPES + 1:
+        return ct_run<CtAccJerk, 2, 256, 1>(L, geff, st);
+    default: return ct_run<CtAccJerk, 1, 128, 4>(L, geff, st);
     }
 }
 
