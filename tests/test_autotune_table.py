@@ -110,3 +110,19 @@ def test_centred_mid_reach_setter():
         assert lib.set_centred_mid(0.0) == 0.0
     finally:
         lib.set_centred_mid(prev)
+
+
+def test_ensemble_default_shape_rejects_bad_shapes():
+    _lib_or_skip()
+    from tupan_gb300 import ensemble as en
+    old = en.default_shape()
+    try:
+        for bad in ((64, 128, 1), (128, 96, 1), (128, 128, 2), (512, 128, 0),
+                    (128, 1024, 0)):
+            with pytest.raises(lib.TupanGB300Error):
+                en.set_default_shape(*bad)
+        assert en.default_shape() == old
+        en.set_default_shape(256, 32, 1)
+        assert en.default_shape() == (256, 32, 1)
+    finally:
+        en.set_default_shape(*old)
