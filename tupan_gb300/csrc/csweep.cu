@@ -32,9 +32,9 @@
 //    (FFMA2/FADD2/FMUL2) evaluates one i against two j, and the i operands,
 //    constant over a tile, are duplicated into register pairs once per tile
 //    instead of duplicating every j operand.
-//  * Sums run in FP32 over runs of 32 j per lane half in far tiles (64 for
-//    the jerk sums; 4 in near tiles), then fold into a Kahan (sum,
-//    correction) pair; the result is formed in
+//  * Sums run in FP32 over runs of 64 j per lane half in far and mid tiles
+//    (128, a whole tile, for the jerk sums; 4 in near tiles), then fold into
+//    a Kahan (sum, correction) pair; the result is formed in
 //    double, scattered back to the caller's particle order.  A grid j-split
 //    writes partial sums that a second kernel reduces in a fixed order.
 //  * Tiles reach shared memory by bulk asynchronous copies (cp.async.bulk)
@@ -689,20 +689,23 @@ __global__ void __launch_bounds__(NT, MINB) ct_sweep(const CtLaunch L)
     // N = 3000 with 8 quads everywhere, 6.3e-7 with 2 quads in near tiles,
     // which is the pair arithmetic's own floor there), so near tiles fold
     // every 2 quads.
-    // Far (and mid) tiles fold the Phi/Acc sums every other run (64
+    // Far (and mid) tiles fold the Phi/Acc sums every fourth run (128
     // records) and the jerk sums (outputs 3..5 of AccJerk, whose bound is
-    // the loose one) every fourth (128): the terms of a far tile are small
+    // the loose one) once per tile (256): the terms of a far tile are small
     // next to the running sum.  Emulated with the kernel's order of FP32
     // runs and Kahan folds (N = 262144 sphere, the 24 particles nearest its
     // centre and 24 random ones, mid form): max |da|/|a| 3.35e-6 with
     // 32-record folds, 3.0e-6 with 64; random particles 3.4e-8 and 3.5e-8.
+    // On the GPU, 128/256-record folds against 64/128: centre particles of
+    // N = 262144 3.4e-6 against 3.8e-6, of N = 2^20 9.0e-7 against 6.3e-7;
+    // AccJerk 0.2 % and Acc 0.6 % faster.
     auto run_tile = [&](const float *F, auto cls_tag, auto uni_tag) {
         constexpr int CLS = decltype(cls_tag)::value;
         constexpr bool NEAR = CLS == CT_NEARBY;
         constexpr bool UNI = decltype(uni_tag)::value;
         constexpr int RUNQ = NEAR ? 2 : 8;
-        constexpr int PA = NEAR ? 1 : 2;     // runs per fold: Phi, Acc sums
-        constexpr int PJ = NEAR ? 1 : 4;     // runs per fold: jerk sums
+        constexpr int PA = NEAR ? 1 : 4;     // runs per fold: Phi, Acc sums
+        constexpr int PJ = NEAR ? 1 : 8;     // runs per fold: jerk sums
         static_assert(CT % (4 * RUNQ * PJ) == 0, "a tile ends on a fold");
         float2 p[NI][NO];
 #pragma unroll
