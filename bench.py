@@ -2,11 +2,14 @@
 
 One step = one Acc sweep and one AccJerk sweep of all N i-particles against
 all N j-particles of a seeded Plummer sphere (equal masses, eps = 1e-4),
-i.e. 2 N^2 pairwise interactions.  ``value`` is interactions per second with
-the particles resident in HBM (device-pointer entry point, CUDA events on the
-launching stream, L2 flushed between steps).  ``e2e`` is the same metric
-through the reference-facing C-ABI (``acc_kernel`` / ``acc_jerk_kernel``)
-from pinned host arrays, copies included.  The roofline line covers the
+i.e. 2 N^2 pairwise interactions (at this size both take the centred
+kernels: Morton-ordered particles, tile-centred records).  ``value`` is
+interactions per second with the particles resident in HBM (device-pointer
+entry point, CUDA events on the launching stream, L2 flushed between
+steps).  ``e2e`` is the same metric through the reference-facing plugin
+object (``extensions.Acc`` / ``AccJerk`` ``.calc(ps, ps)`` on ordinary
+pageable numpy arrays -> ``CUDAKernel.run`` -> the ``acc_kernel`` /
+``acc_jerk_kernel`` C-ABI), copies included.  The roofline line covers the
 dominant kernel, the AccJerk sweep, against the FP32 FMA throughput measured
 in the same run.  The FP64 (EXACT) path's rate is measured on an i-subset
 (the cost is exactly linear in ni) for the SPLIT / FP64 ratio.
