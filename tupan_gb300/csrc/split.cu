@@ -14,6 +14,9 @@
 //    (TMA, cp.async.bulk) into a two-stage ring guarded by mbarriers; i-data
 //    stay in registers.
 //
+// Phi, Acc and AccJerk sweeps of at least 2^31 interactions take the
+// centred kernels of csweep.cu instead (run_device_sweep in abi.cu decides).
+//
 // The j - i sign convention is used throughout (the reference forms i - j
 // and subtracts); every output is the same quantity.
 
