@@ -210,3 +210,38 @@ def check_configuration_size(n, k, centre_rel=1e-5):
     got_a = run_centred("acc_kernel", ps, ps, policy=-1)
     ea = vec_rel_err(tuple(g[idx] for g in got_a), want_a, (0, 1, 2))
     assert ea[k:].max() <= 1e-6 and ea[:k].max() <= centre_rel
+
+
+def test_every_particle_of_the_bench_sphere():
+    # All 262144 particles of the bench's sphere (seed 2024 Plummer, eps
+    # 1e-4): the centred AccJerk sweep against the fp64 EXACT sweep on the
+    # GPU (bit-identical to the reference's fp64 kernel, pinned by the
+    # parity tests).  Bounds: median |da|/|a| <= 1e-7; at most 1 in 10^4
+    # particles above 1e-6 (the near-cancelling ones at the centre), none
+    # above 1e-5; jerk median <= 1e-6.
+    torch = pytest.importorskip("torch")
+    n = 262144
+    ps = ics.plummer(n, eps=1e-4, seed=2024)
+    names = ("m", "rx", "ry", "rz", "e2", "vx", "vy", "vz")
+    d = {k: torch.from_numpy(np.ascontiguousarray(ps[k])).cuda()
+         for k in names}
+    p = [d[k].data_ptr() for k in names]
+    res = {}
+    for mode in (lib.MODE_SPLIT, lib.MODE_EXACT):
+        out = [torch.empty(n, dtype=torch.float64, device="cuda")
+               for _ in range(6)]
+        lib.dev_sweep("acc_jerk_kernel", n, p, n, p,
+                      [o.data_ptr() for o in out], mode=mode)
+        torch.cuda.synchronize()
+        lib.check()
+        res[mode] = [o.cpu().numpy() for o in out]
+    got, want = res[lib.MODE_SPLIT], res[lib.MODE_EXACT]
+    ea = vec_rel_err(got, want, (0, 1, 2))
+    ej = vec_rel_err(got, want, (3, 4, 5))
+    above = int((ea > 1e-6).sum())
+    print("all %d: acc max %.3g median %.3g, above 1e-6: %d; jerk max %.3g "
+          "median %.3g" % (n, ea.max(), np.median(ea), above, ej.max(),
+                           np.median(ej)))
+    assert np.median(ea) <= 1e-7
+    assert above <= n // 10000 and ea.max() <= 1e-5
+    assert np.median(ej) <= 1e-6
