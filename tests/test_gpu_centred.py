@@ -158,7 +158,7 @@ def test_centred_configuration_sizes(n, k):
 
 def test_centred_configuration_size_without_mid_tiles():
     # the one-operation far difference on every tile beyond 1.25 R: the
-    # centre particles' relative bound doubles (measured 9.7e-6)
+    # centre particles' relative bound doubles (measured 7.9e-6 to 9.7e-6)
     prev = lib.set_centred_mid(0.0)
     try:
         check_configuration_size(262144, 256, centre_rel=2e-5)
