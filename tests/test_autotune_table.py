@@ -126,3 +126,16 @@ def test_ensemble_default_shape_rejects_bad_shapes():
         assert en.default_shape() == (256, 32, 1)
     finally:
         en.set_default_shape(*old)
+
+
+def test_apply_saved_lenient_skips_a_bad_entry(tmp_path, monkeypatch):
+    # what the library's load does: a stale entry is skipped with a warning
+    _lib_or_skip()
+    path = _write(tmp_path, {"Fake GPU": {
+        "acc_jerk_kernel|1024|65536": {"variant": 999, "gsplit": 1,
+                                       "seconds": 1e-4},
+        "acc_kernel|1024|65536": {"variant": 4, "gsplit": 8,
+                                  "seconds": 1e-4}}})
+    monkeypatch.setattr(autotune, "_device_name", lambda: "Fake GPU")
+    with pytest.warns(UserWarning):
+        assert autotune.apply_saved(path, strict=False) == 1

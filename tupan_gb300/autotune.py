@@ -170,27 +170,45 @@ def save(table, path=TABLE):
         json.dump(allt, f, indent=1, sort_keys=True)
 
 
-def apply_saved(path=TABLE):
-    """Record the saved entries of this GPU in the library's table."""
+def apply_saved(path=TABLE, strict=True):
+    """Record the saved entries of this GPU in the library's table; returns
+    how many were taken.  strict: a malformed or unusable entry raises;
+    otherwise it is skipped with a warning (the library's load does this, so
+    a stale table never makes the library unusable)."""
     if not os.path.exists(path):
         return 0
     with open(path) as f:
         allt = json.load(f)
     entries = allt.get(_device_name(), {})
     ens = []
+    taken = 0
     for key, e in entries.items():
-        parts = key.split("|")
-        if parts[0] == "ensemble":
-            ens.append((int(parts[1]), e))
-            continue
-        k, ni, nj = parts
-        lib.set_tuned(k, int(ni), int(nj), e["variant"], e["gsplit"])
+        try:
+            parts = key.split("|")
+            if parts[0] == "ensemble":
+                ens.append((int(parts[1]), e))
+                continue
+            k, ni, nj = parts
+            lib.set_tuned(k, int(ni), int(nj), e["variant"], e["gsplit"])
+            taken += 1
+        except (ValueError, KeyError, lib.TupanGB300Error) as exc:
+            if strict:
+                raise
+            import warnings
+            warnings.warn("tuning entry %r skipped: %s" % (key, exc))
     if ens:
         # the entry measured on the most systems sets the default shape
         from .ensemble import set_default_shape
         e = max(ens, key=lambda x: x[0])[1]
-        set_default_shape(e["nt"], e["ib"], e["prefetch"])
-    return len(entries)
+        try:
+            set_default_shape(e["nt"], e["ib"], e["prefetch"])
+            taken += len(ens)
+        except (KeyError, lib.TupanGB300Error) as exc:
+            if strict:
+                raise
+            import warnings
+            warnings.warn("ensemble tuning entry skipped: %s" % exc)
+    return taken
 
 
 def main(argv=None):

@@ -112,7 +112,11 @@ def _apply_tuning():
     if device_name() is None:
         return
     from . import autotune
-    autotune.apply_saved()
+    try:
+        autotune.apply_saved(strict=False)
+    except (OSError, ValueError) as exc:      # an unreadable table
+        import warnings
+        warnings.warn("tuning table not applied: %s" % exc)
 
 
 def device_name():
